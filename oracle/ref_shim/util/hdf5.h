@@ -1,0 +1,3 @@
+// TEST INFRASTRUCTURE: empty stand-in (not used on the compiled path)
+#pragma once
+#include "util/stats.h"
