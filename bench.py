@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the headline workload: SU(3) Wilson HMC on a 32^4 lattice,
+beta = 6.0, Omelyan (2mn) integrator with epsilon = 0.5 and 20 substeps
+(tau = 1), mixed precision (FP32 links, momenta and force; FP64 action and
+Hamiltonian sums, dH and Metropolis on the device), after thermalisation from
+a hot start with seed 7. One step = one HMC trajectory; the metric is
+trajectories per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica chain on its own
+GPU (the path has no exchange step: replicas only); value = total
+trajectories of all ranks / max over ranks of the timed region.
+
+--impl reference times the reference's algorithm on the host CPU cores: the
+C++ restatement of src/gauge + src/lattice (oracle/, compiled with g++
+-fopenmp), one momentum step + one link update + one plaquette of the same
+32^4 FP32 fields per step, extrapolated to a trajectory.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(name="su3_hmc_32^4_beta6.0_2mn_eps0.5_n20_mixed", group=3, dims=[32, 32, 32, 32], beta=6.0,
+                scheme="2mn", eps=0.5, substeps=20, seed=7, therm=200)
+METRIC = "SU(3) 32^4 HMC trajectories/s"
+UNIT = "traj/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--therm", type=int, default=WORKLOAD["therm"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def sizes(dims, prec_bytes=4):
+    V = 1
+    for d in dims:
+        V *= d
+    nd = len(dims)
+    U = nd * V * 18 * prec_bytes
+    P = nd * V * 8 * prec_bytes
+    return V, U, P
+
+
+def deltas_counts(n):
+    n_u = (n + 1) // 2
+    return n_u, n - n_u
+
+
+def algorithmic_bytes_per_traj(dims, n):
+    """Compulsory HBM bytes of one trajectory, every object read/written once:
+    n_P (|U| + 2|P|) + n_U (2|U| + |P|) + |P| + 2(|U| + |P|) + 2|U|."""
+    _, U, P = sizes(dims)
+    n_u, n_p = deltas_counts(n)
+    return n_p * (U + 2 * P) + n_u * (2 * U + P) + P + 2 * (U + P) + 2 * U
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per launch of the force kernel from the committed ncu
+    summary, scaled to the 32^4 launch (null when absent)."""
+    p = os.path.join(ROOT, "profiles", "momentum_step_su3_f32.md")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch_32^4:"):
+                return float(line.split(":")[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples (every 200 ms) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_md(U_host, P_host, dims, n, beta, delta, threads=0):
+    """The reference algorithm (oracle restatement) on the host cores: one
+    momentum step + one link update + one plaquette on the full lattice,
+    extrapolated to a trajectory of n_P momentum and n_U link steps plus two
+    actions, a momentum refresh and a reunitisation (each costed as a link
+    update)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    cores = pyoracle.set_threads(threads)
+    tf, te, tp = pyoracle.bench_md(WORKLOAD["group"], 1, dims, U_host, P_host, beta, delta, 1)
+    n_u, n_p = deltas_counts(n)
+    t_traj = n_p * tf + (n_u + 2) * te + 2 * tp
+    return 1.0 / t_traj, cores, tf, te, tp
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    dims, n = WORKLOAD["dims"], 0
+    d = pyoracle.make_deltas(WORKLOAD["scheme"], WORKLOAD["eps"], WORKLOAD["substeps"])
+    n = len(d)
+    U = pyoracle.random_gauge(3, 1, dims, WORKLOAD["seed"])
+    P = pyoracle.random_momenta(3, 1, dims, WORKLOAD["seed"], 0)
+    vals = []
+    for k in range(args.warmup + args.steps):
+        v, cores, tf, te, tp = cpu_baseline_md(U, P, dims, n, WORKLOAD["beta"], float(d[1]))
+        if k >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    sample = (f"per step: one momentum step ({tf:.2f} s), one link update ({te:.2f} s) and one plaquette "
+              f"({tp:.2f} s) of the reference algorithm on the full 32^4 SU(3) FP32 lattice, extrapolated to a "
+              f"{WORKLOAD['scheme']} n={WORKLOAD['substeps']} trajectory")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD["name"], "lattice": dims, "beta": WORKLOAD["beta"],
+                       "integrator": f"{WORKLOAD['scheme']} eps={WORKLOAD['eps']} n={WORKLOAD['substeps']}",
+                       "parallelism": "cpu threads"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import mesh_gb300 as mg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    mg.load()
+    stream = torch.cuda.Stream()
+    ctx = mg.Context(local, stream.cuda_stream)
+    dims = WORKLOAD["dims"]
+    grid = mg.Grid(dims)
+    beta = WORKLOAD["beta"]
+    d = mg.make_deltas(WORKLOAD["scheme"], WORKLOAD["eps"], WORKLOAD["substeps"])
+    n = len(d)
+    n_u, n_p = deltas_counts(n)
+    launches_per_traj = 1 + n_u + n_p + 1 + 2  # refresh, link updates, momentum steps, plaquette, metropolis, copy
+    h = mg.Hmc(ctx, WORKLOAD["group"], mg.F32, grid, seed=WORKLOAD["seed"] + rank)
+    h.randomize_gauge_field()
+    h.run(beta, d, args.therm, use_graph=True)
+    h.run(beta, d, args.warmup, use_graph=True)
+    ctx.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    clocks = Clocks(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    h.run(beta, d, args.steps, use_graph=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1000.0)
+    hist = h.history(h.count - args.steps - args.warmup - args.therm)
+    acc = float(np.mean(hist["accept_history"][-args.steps:]))
+    plaq = float(np.mean(hist["plaq_history"][args.therm:]))
+    edH = float(np.mean(np.exp(-hist["deltaH_history"][args.therm:])))
+
+    # dominant kernel: the fused momentum step (staples + force + P update),
+    # timed alone with CUDA events on the launching stream
+    _, Ub, Pb = sizes(dims)
+    B_f = Ub + 2 * Pb
+    U, P = h.U, h.P
+    reps = 20
+    for _ in range(3):
+        mg.momentum_step(P, U, beta, 1e-9)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(reps):
+        mg.momentum_step(P, U, beta, 1e-9)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_force = f0.elapsed_time(f1) / reps / 1000.0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        mg.evolve(U, P, 0.0)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t_evolve = ev0.elapsed_time(ev1) / reps / 1000.0
+    peak, peak_kind = measured_peaks()
+    achieved = B_f / t_force / 1e9
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": WORKLOAD["name"], "lattice": dims, "beta": beta,
+                      "integrator": f"{WORKLOAD['scheme']} eps={WORKLOAD['eps']} n={WORKLOAD['substeps']}",
+                      "precision": "FP32 links/momenta/force, FP64 sums/dH/Metropolis",
+                      "thermalisation": f"{args.therm} trajectories from a hot start, seed {WORKLOAD['seed']}",
+                      "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                      "l2": "inputs larger than L2 (links 302 MB + momenta 134 MB > 129 MB)",
+                      "timing": "CUDA events on the launching stream, CUDA-graph replay of whole trajectories"},
+           "physics": {"acceptance": acc, "plaquette_mean": plaq, "exp_minus_dH_mean": edH},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": ncu_traffic(),
+                        "kernel": "k_momentum_step<SU3,float,4> (fused staples+force+momentum update)",
+                        "algorithmic_bytes_per_launch": B_f, "avg_launch_ms": t_force * 1e3,
+                        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                        else "fallback 6.8 TB/s"},
+           "kernels": {"link_update_ms": t_evolve * 1e3,
+                       "link_update_GBps": (2 * Ub + Pb) / t_evolve / 1e9,
+                       "trajectory_algorithmic_GB": algorithmic_bytes_per_traj(dims, n) / 1e9,
+                       "trajectory_effective_GBps": algorithmic_bytes_per_traj(dims, n) / (ms / args.steps / 1e3)
+                       / 1e9},
+           "clocks": clk, "gpu_launches": launches_per_traj * args.steps}
+
+    # end to end through the C ABI with host buffers: the gauge field in the
+    # reference's host layout is imported, one trajectory runs, the field is
+    # exported back (pinned host memory), every step
+    if not args.no_e2e:
+        host_t = torch.empty((len(dims), grid.size, 18), dtype=torch.float32, pin_memory=True)
+        host = host_t.numpy()
+        host[...] = U.export()
+        k_e2e = max(3, min(args.steps, 10))
+        h.run_host(host, beta, d, 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            h.run_host(host, beta, d, 1)
+        t_e2e = (time.perf_counter() - t0) / k_e2e
+        out["e2e"] = {"value": world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": host.nbytes,
+                      "d2h_bytes_per_step": host.nbytes + 40, "steps": k_e2e,
+                      "api": "mesh_hmc_run_host (import U, one trajectory, export U)"}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        Uh = U.export()
+        Ph = P.export()
+        v, cores, tf, te, tp = cpu_baseline_md(Uh, Ph, dims, n, beta, float(d[1]))
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"one momentum step ({tf:.2f} s), one link update ({te:.2f} s), one "
+                                         f"plaquette ({tp:.2f} s) of the reference algorithm (oracle/ C++ "
+                                         f"restatement, FP32) on the full 32^4 lattice, extrapolated to a trajectory"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    h.close()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

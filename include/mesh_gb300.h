@@ -1,0 +1,222 @@
+/*
+ * mesh_gb300 — C ABI of the GB300 (sm_103a) lattice-gauge hot path.
+ *
+ * Drop-in boundary for krox/mesh's lattice_apply/reduction layer
+ * (src/lattice), pure-gauge HMC (src/gauge/utils.h, hmc.h, hmc.cpp) and
+ * Landau gauge fixing (src/gauge/landau.h). The reference exposes header
+ * templates (Lattice<T>, GaugeField<G>, Hmc<G>, Landau<G>) and throws
+ * std::runtime_error on CUDA errors (src/lattice/device.cpp:11-18); here every
+ * entry point returns an int status (0 = MESH_OK) and never throws. The C++
+ * wrapper include/mesh/mesh.hpp restores the reference's class names and
+ * rethrows non-zero statuses as std::runtime_error.
+ *
+ * Conventions
+ *  - group: MESH_U1, MESH_SU2, MESH_SU3 and precision MESH_F32 (float),
+ *    MESH_F64 (double) are dispatchByGroup's runtime choices
+ *    (src/gauge/utils.h:156-186; precision 1 = float, 2 = double).
+ *  - Host buffers use the reference's host layout: sites lexicographic with
+ *    dimension 0 slowest (src/lattice/grid.h:39-49), one block of V objects
+ *    per stacked component mu (LatticeStack, src/lattice/lattice.h:159-192),
+ *    objects as complex (re,im), quaternion (re,im1,im2,im3) or row-major
+ *    3x3 complex matrices. Momenta/forces are algebra fields: on the host they
+ *    are full group-type objects (as the reference stores them); on the
+ *    device they are packed (1/3/8 reals).
+ *  - Device storage is even/odd checkerboard, structure-of-arrays
+ *    (mesh_field_device_ptr documents nothing more: treat it as opaque).
+ *  - All extents must be even, 2 <= nd <= 4, and the volume < 2^31.
+ *  - Calls are issued on the context's stream. Functions returning a host
+ *    scalar synchronise that stream (as the reference's reductions do,
+ *    src/lattice/device.h:259-260); the others are asynchronous.
+ *  - Not thread-safe per context (like the reference's globals).
+ */
+#ifndef MESH_GB300_H
+#define MESH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MESH_OK 0
+#define MESH_ERR_ARG 1         /* invalid argument (shape, group, size, kind) */
+#define MESH_ERR_CUDA 2        /* CUDA runtime error (device.cpp:11-18 analogue) */
+#define MESH_ERR_STATE 3       /* objects on different grids/contexts, wrong state */
+#define MESH_ERR_TIMEOUT 4     /* a bounded device-side wait expired */
+#define MESH_ERR_NUMERIC 5     /* NaN/Inf in an action, Hamiltonian or theta */
+#define MESH_ERR_NOCONV 6      /* iteration limit reached without convergence */
+#define MESH_ERR_UNSUPPORTED 7 /* valid request this build does not implement */
+
+#define MESH_U1 1
+#define MESH_SU2 2
+#define MESH_SU3 3
+#define MESH_F32 1
+#define MESH_F64 2
+
+#define MESH_GROUP 0   /* field of group elements (links, gauge transforms) */
+#define MESH_ALGEBRA 1 /* field of algebra elements (momenta, forces) */
+
+typedef struct mesh_ctx_s *mesh_ctx;
+typedef struct mesh_field_s *mesh_field;
+typedef struct mesh_hmc_s *mesh_hmc;
+
+/* ---- library ------------------------------------------------------------ */
+/* last error message of the calling thread (valid until the next call) */
+const char *mesh_last_error(void);
+/* ABI version: major*10000 + minor*100 + patch */
+int mesh_version(void);
+
+/* ---- context: device + stream + reduction scratch ------------------------
+ * Replaces the reference's implicit "current device, default stream"
+ * (src/lattice/device.h:219-228). stream == NULL: the context creates and
+ * owns a non-blocking stream. */
+int mesh_ctx_create(int device, void *stream, mesh_ctx *out);
+int mesh_ctx_destroy(mesh_ctx ctx);
+int mesh_ctx_synchronize(mesh_ctx ctx);
+/* the cudaStream_t the context launches on */
+void *mesh_ctx_stream(mesh_ctx ctx);
+
+/* ---- fields: Lattice<T> / LatticeStack<T> / GaugeField<G> ---------------
+ * Replaces Lattice<T>(Grid) and LatticeStack<T>(Grid)
+ * (src/lattice/lattice.h:43-47,171-176; GaugeField = LatticeStack,
+ * src/gauge/utils.h:21). nstack = number of stacked components (nd for a
+ * gauge field or momenta, 1 for a single Lattice). Contents are
+ * uninitialised, as in the reference. */
+int mesh_field_create(mesh_ctx ctx, int kind, int group, int precision, int nd, const int32_t *dims, int nstack,
+                      mesh_field *out);
+int mesh_field_destroy(mesh_field f);
+int mesh_field_info(mesh_field f, int *kind, int *group, int *precision, int *nd, int32_t *dims, int *nstack);
+/* size in bytes of the field in the reference's host layout */
+size_t mesh_field_host_bytes(mesh_field f);
+/* Lattice::copy_from_host / copy_to_host (lattice.h:102-115), for every
+ * stacked component; the layout conversion is a bit-exact permutation. */
+int mesh_field_import(mesh_field f, const void *host, size_t bytes);
+int mesh_field_export(mesh_field f, void *host, size_t bytes);
+/* deep copy (Lattice copy assignment, lattice.h:83-93); same shape required */
+int mesh_field_copy(mesh_field dst, mesh_field src);
+/* Lattice::zeros / fill_zeros (lattice.h:51-58) */
+int mesh_field_set_zero(mesh_field f);
+/* group fields: every element = identity (cold start; the reference's
+ * Landau::reset g.fill(G(1)), landau.h:14) */
+int mesh_field_set_unit(mesh_field f);
+/* group fields: Haar-random elements (random_gauge_field, utils.h:43-70);
+ * algebra fields: Gaussian momenta with tr(T^aT^b)=delta/2
+ * (random_algebra_field, utils.h:54-78). Drawn on the device from a
+ * counter-based stream (seed, counter); no host RNG, no H2D copy. */
+int mesh_field_random(mesh_field f, uint64_t seed, uint64_t counter);
+/* opaque device storage (even/odd structure of arrays) */
+void *mesh_field_device_ptr(mesh_field f);
+
+/* ---- lattice_apply layer on single-component group fields ----------------
+ * The named site-wise operations the gauge code builds from lattice_apply
+ * (src/lattice/lattice.h:256-364, src/gauge/utils.h:28-33). */
+/* dst[x] = src[x + offset * e_dir], periodic (cshift, lattice.h:366-389) */
+int mesh_site_cshift(mesh_field dst, mesh_field src, int dir, int offset);
+/* dst = a * b (MESH_DEFINE_LATTICE_BINARY(*), lattice.h:289-301) */
+int mesh_site_mul(mesh_field dst, mesh_field a, mesh_field b);
+/* dst = adj(a) (utils.h:31) */
+int mesh_site_adj(mesh_field dst, mesh_field a);
+/* sum_x real_trace(a(x)) in FP64 (sum_real_trace, utils.h:29) */
+int mesh_site_sum_real_trace(mesh_field a, double *out);
+/* sum of norm2 over every component (norm2(LatticeStack), utils.h:35-41);
+ * algebra fields use the kinetic (defining-representation Frobenius) norm */
+int mesh_field_norm2(mesh_field a, double *out);
+
+/* ---- gauge utilities (src/gauge/utils.h) --------------------------------- */
+/* plaquette normalised to [0,1] (utils.h:94-108); FP64 accumulation */
+int mesh_plaquette(mesh_field U, double *out);
+/* Wilson action (1 - plaquette) * beta * Nd(Nd-1)/2 * V (utils.h:141-146) */
+int mesh_wilson_action(mesh_field U, double beta, double *out);
+/* S = staple sum for direction mu (stapleSum, utils.h:114-139); S is a
+ * single-component group field on U's grid */
+int mesh_staple_sum(mesh_field S, mesh_field U, int mu);
+/* F = project_on_algebra(U_mu * S_mu * beta / (2 Nc)) (wilsonDeriv,
+ * utils.h:148-153); F is a single-component algebra field */
+int mesh_wilson_deriv(mesh_field F, mesh_field U, int mu, double beta);
+/* project_on_group_fast on every link (reunitize, utils.h:80-91) */
+int mesh_reunitize(mesh_field U);
+
+/* ---- HMC building blocks (src/gauge/hmc.h, hmc.cpp) ---------------------- */
+/* U_mu <- exp(project_on_algebra(P_mu) * t) U_mu for all mu (evolve,
+ * hmc.h:249-257) */
+int mesh_evolve(mesh_field U, mesh_field P, double t);
+/* P_mu -= wilsonDeriv(U, mu, beta) * delta for all mu (the momentum step
+ * of runHmd, hmc.h:276-278), fused: staples, product, projection and update
+ * in one kernel */
+int mesh_momentum_step(mesh_field P, mesh_field U, double beta, double delta);
+/* runHmd (hmc.h:261-280): alternating position/momentum steps */
+int mesh_run_hmd(mesh_field U, mesh_field P, double beta, const double *deltas, int n);
+/* makeDeltas (hmc.cpp:7-51): scheme "2lf", "2mn" or "4mn"; writes at most
+ * capacity values and the count to *n */
+int mesh_make_deltas(const char *scheme, double epsilon, int substeps, double *out, int capacity, int *n);
+
+/* ---- HMC chain: Hmc<G> (hmc.h:287-336, hmc.cpp:394-445) ------------------
+ * Owns U, P and the proposal U_new. Momenta and the Metropolis uniform come
+ * from counter-based device streams keyed by `seed` and the trajectory
+ * number; H_old/H_new, dH and the accept decision are computed on the device
+ * in FP64. */
+typedef struct mesh_hmc_record
+{
+	double plaquette; /* plaquette(U) after the accept/reject step */
+	double dH;        /* H_new - H_old */
+	double accept;    /* 1.0 accepted, 0.0 rejected */
+	double H_old, H_new;
+} mesh_hmc_record;
+
+int mesh_hmc_create(mesh_ctx ctx, int group, int precision, int nd, const int32_t *dims, uint64_t seed,
+                    mesh_hmc *out);
+int mesh_hmc_destroy(mesh_hmc h);
+/* borrowed handles of the state: which = 0 -> U, 1 -> P */
+int mesh_hmc_field(mesh_hmc h, int which, mesh_field *out);
+/* randomizeGaugeField (hmc.cpp:397-400) and a cold start */
+int mesh_hmc_randomize(mesh_hmc h);
+int mesh_hmc_cold_start(mesh_hmc h);
+/* runHmcUpdate (hmc.cpp:413-445): one trajectory, synchronous, record out */
+int mesh_hmc_update(mesh_hmc h, double beta, const double *deltas, int n, mesh_hmc_record *rec);
+/* One trajectory on caller-supplied momenta P0 (algebra field, copied, not
+ * modified) and Metropolis uniform: the parity entry point. */
+int mesh_hmc_update_supplied(mesh_hmc h, mesh_field P0, double uniform, double beta, const double *deltas, int n,
+                             mesh_hmc_record *rec);
+/* `count` trajectories without host synchronisation. use_graph != 0
+ * captures one trajectory in a CUDA graph and replays it. Records go to a
+ * device history read by mesh_hmc_history. */
+int mesh_hmc_run(mesh_hmc h, double beta, const double *deltas, int n, int count, int use_graph);
+/* number of trajectories recorded so far */
+int mesh_hmc_count(mesh_hmc h, int *n);
+/* copy records [first, first+count) to host arrays (any may be NULL) */
+int mesh_hmc_history(mesh_hmc h, int first, int count, double *plaquette, double *dH, double *accept);
+/* HMC with the gauge field exchanged in the reference's host layout every
+ * call: import U from host, run `count` trajectories, export U to host. */
+int mesh_hmc_run_host(mesh_hmc h, void *host_U, size_t bytes, double beta, const double *deltas, int n, int count,
+                      mesh_hmc_record *last);
+
+/* ---- Landau gauge fixing (src/gauge/landau.h) ----------------------------
+ * g is a single-component group field (the gauge transform); U is not
+ * modified. */
+/* functional sum_mu sum_x ReTr(g(x) U_mu(x) g(x+mu)^dagger)/(Nc Nd V)
+ * (Landau::operator(), landau.h:23-32), FP64 */
+int mesh_landau_functional(mesh_field U, mesh_field g, double *out);
+/* theta_ref = sum_x |Delta(x)|^2 / (Nd V), Delta = sum_mu A_mu(x)-A_mu(x-mu)
+ * (Landau::condition, landau.h:37-49), FP64 */
+int mesh_landau_theta(mesh_field U, mesh_field g, double *out);
+/* F = project_on_algebra(g d) * (-0.5/(Nc Nd V)) (Landau::deriv,
+ * landau.h:52-65); F a single-component algebra field */
+int mesh_landau_deriv(mesh_field F, mesh_field U, mesh_field g);
+/* the reference's nonlinear CG with line search (Landau::run,
+ * landau.h:100-136) with the stopping threshold as an argument */
+int mesh_landau_cg(mesh_field U, mesh_field g, int max_iter, double tol, int *iters, double *theta);
+/* checkerboard overrelaxation (no reference counterpart; the legacy
+ * relaxation of src/old/gauge_fixing.cpp:33-79 overrelaxed): sweeps in
+ * blocks of check_every, theta_ref after each block, stop below tol */
+int mesh_landau_or(mesh_field U, mesh_field g, double omega, double tol, int max_sweeps, int check_every,
+                   int *sweeps, double *theta);
+/* U <- g U g^dagger(x+mu) for all mu (apply a gauge transform) */
+int mesh_gauge_transform(mesh_field U, mesh_field g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MESH_GB300_H */

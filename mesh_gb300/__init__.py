@@ -1,0 +1,498 @@
+"""mesh_gb300 — GB300 (sm_103a) implementation of krox/mesh's lattice-gauge
+hot path, behind a C ABI (include/mesh_gb300.h).
+
+This package is the Python host side used by the tests and the benchmark: a
+ctypes binding of libmesh_gb300.so with classes named after the reference's
+C++ API (src/lattice/lattice.h, src/gauge/utils.h, hmc.h, landau.h):
+``Grid``, ``Lattice``, ``GaugeField``, ``Hmc``, ``Landau``, ``make_deltas``,
+``plaquette``, ``wilson_action``, ``staple_sum``, ``wilson_deriv``,
+``reunitize``, ``evolve``, ``run_hmd``, ``cshift``.
+
+Host arrays use the reference's host layout: a gauge field is a numpy array
+``(nd, V, nreal)`` (sites lexicographic, dimension 0 slowest), a single
+lattice ``(V, nreal)``; momenta/forces are full group-type objects on the host
+(complex / quaternion / 3x3 complex matrix), packed algebra on the device.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is present,
+creating a ``Context`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmesh_gb300.so")
+
+U1, SU2, SU3 = 1, 2, 3
+F32, F64 = 1, 2
+GROUP, ALGEBRA = 0, 1
+GROUP_NAMES = {"u1": U1, "su2": SU2, "su3": SU3}
+NREAL = {U1: 2, SU2: 4, SU3: 18}
+NALG = {U1: 1, SU2: 3, SU3: 8}
+NC = {U1: 1, SU2: 2, SU3: 3}
+
+STATUS = {
+    0: "MESH_OK", 1: "MESH_ERR_ARG", 2: "MESH_ERR_CUDA", 3: "MESH_ERR_STATE", 4: "MESH_ERR_TIMEOUT",
+    5: "MESH_ERR_NUMERIC", 6: "MESH_ERR_NOCONV", 7: "MESH_ERR_UNSUPPORTED",
+}
+
+# every symbol declared in include/mesh_gb300.h, with its ctypes signature
+_P, _I, _D, _U64, _SZ = C.c_void_p, C.c_int, C.c_double, C.c_uint64, C.c_size_t
+_IP, _DP, _I32P = C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int32)
+_PP = C.POINTER(C.c_void_p)
+
+
+class HmcRecord(C.Structure):
+    _fields_ = [("plaquette", C.c_double), ("dH", C.c_double), ("accept", C.c_double),
+                ("H_old", C.c_double), ("H_new", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SIGNATURES = {
+    "mesh_last_error": (C.c_char_p, []),
+    "mesh_version": (_I, []),
+    "mesh_ctx_create": (_I, [_I, _P, _PP]),
+    "mesh_ctx_destroy": (_I, [_P]),
+    "mesh_ctx_synchronize": (_I, [_P]),
+    "mesh_ctx_stream": (_P, [_P]),
+    "mesh_field_create": (_I, [_P, _I, _I, _I, _I, _I32P, _I, _PP]),
+    "mesh_field_destroy": (_I, [_P]),
+    "mesh_field_info": (_I, [_P, _IP, _IP, _IP, _IP, _I32P, _IP]),
+    "mesh_field_host_bytes": (_SZ, [_P]),
+    "mesh_field_import": (_I, [_P, _P, _SZ]),
+    "mesh_field_export": (_I, [_P, _P, _SZ]),
+    "mesh_field_copy": (_I, [_P, _P]),
+    "mesh_field_set_zero": (_I, [_P]),
+    "mesh_field_set_unit": (_I, [_P]),
+    "mesh_field_random": (_I, [_P, _U64, _U64]),
+    "mesh_field_device_ptr": (_P, [_P]),
+    "mesh_site_cshift": (_I, [_P, _P, _I, _I]),
+    "mesh_site_mul": (_I, [_P, _P, _P]),
+    "mesh_site_adj": (_I, [_P, _P]),
+    "mesh_site_sum_real_trace": (_I, [_P, _DP]),
+    "mesh_field_norm2": (_I, [_P, _DP]),
+    "mesh_plaquette": (_I, [_P, _DP]),
+    "mesh_wilson_action": (_I, [_P, _D, _DP]),
+    "mesh_staple_sum": (_I, [_P, _P, _I]),
+    "mesh_wilson_deriv": (_I, [_P, _P, _I, _D]),
+    "mesh_reunitize": (_I, [_P]),
+    "mesh_evolve": (_I, [_P, _P, _D]),
+    "mesh_momentum_step": (_I, [_P, _P, _D, _D]),
+    "mesh_run_hmd": (_I, [_P, _P, _D, _DP, _I]),
+    "mesh_make_deltas": (_I, [C.c_char_p, _D, _I, _DP, _I, _IP]),
+    "mesh_hmc_create": (_I, [_P, _I, _I, _I, _I32P, _U64, _PP]),
+    "mesh_hmc_destroy": (_I, [_P]),
+    "mesh_hmc_field": (_I, [_P, _I, _PP]),
+    "mesh_hmc_randomize": (_I, [_P]),
+    "mesh_hmc_cold_start": (_I, [_P]),
+    "mesh_hmc_update": (_I, [_P, _D, _DP, _I, C.POINTER(HmcRecord)]),
+    "mesh_hmc_update_supplied": (_I, [_P, _P, _D, _D, _DP, _I, C.POINTER(HmcRecord)]),
+    "mesh_hmc_run": (_I, [_P, _D, _DP, _I, _I, _I]),
+    "mesh_hmc_count": (_I, [_P, _IP]),
+    "mesh_hmc_history": (_I, [_P, _I, _I, _DP, _DP, _DP]),
+    "mesh_hmc_run_host": (_I, [_P, _P, _SZ, _D, _DP, _I, _I, C.POINTER(HmcRecord)]),
+    "mesh_landau_functional": (_I, [_P, _P, _DP]),
+    "mesh_landau_theta": (_I, [_P, _P, _DP]),
+    "mesh_landau_deriv": (_I, [_P, _P, _P]),
+    "mesh_landau_cg": (_I, [_P, _P, _I, _D, _IP, _DP]),
+    "mesh_landau_or": (_I, [_P, _P, _D, _D, _I, _I, _IP, _DP]),
+    "mesh_gauge_transform": (_I, [_P, _P]),
+}
+
+_lib = None
+
+
+class MeshError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Load libmesh_gb300.so (in-tree). Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m mesh_gb300.build`")
+        from . import build as _b
+        _b.build()
+    L = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _chk(rc):
+    if rc != 0:
+        raise MeshError(rc, load().mesh_last_error().decode())
+
+
+def _dims(shape):
+    return (C.c_int32 * len(shape))(*[int(x) for x in shape])
+
+
+def _darr(x):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    return a, a.ctypes.data_as(_DP)
+
+
+def group_code(g) -> int:
+    return GROUP_NAMES[g] if isinstance(g, str) else int(g)
+
+
+def real_dtype(prec):
+    return np.float32 if prec == F32 else np.float64
+
+
+# ---------------------------------------------------------------------------
+class Context:
+    """Device + stream + reduction scratch (mesh_ctx)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        L = load()
+        h = C.c_void_p()
+        _chk(L.mesh_ctx_create(device, C.c_void_p(stream) if stream else None, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    @property
+    def stream(self) -> int:
+        return load().mesh_ctx_stream(self.h) or 0
+
+    def synchronize(self):
+        _chk(load().mesh_ctx_synchronize(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mesh_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass(frozen=True)
+class Grid:
+    """Lattice shape, lexicographic with dimension 0 slowest (grid.h:11-58)."""
+    shape: tuple
+
+    def __init__(self, shape):
+        object.__setattr__(self, "shape", tuple(int(x) for x in shape))
+
+    @property
+    def ndim(self):
+        return len(self.shape)
+
+    @property
+    def size(self):
+        return int(np.prod(self.shape))
+
+
+class Field:
+    """A device field: nstack components of V group or algebra objects."""
+
+    def __init__(self, ctx: Context, kind: int, group, prec: int, grid: Grid, nstack: int):
+        self.ctx, self.kind, self.group, self.prec = ctx, kind, group_code(group), prec
+        self.grid, self.nstack = grid, nstack
+        h = C.c_void_p()
+        _chk(load().mesh_field_create(ctx.h, kind, self.group, prec, grid.ndim, _dims(grid.shape), nstack,
+                                      C.byref(h)))
+        self.h = h
+
+    def _host_shape(self):
+        return (self.nstack, self.grid.size, NREAL[self.group])
+
+    def import_(self, arr):
+        a = np.ascontiguousarray(np.asarray(arr, dtype=real_dtype(self.prec)))
+        assert a.size == int(np.prod(self._host_shape())), "host array size does not match the field"
+        _chk(load().mesh_field_import(self.h, a.ctypes.data_as(C.c_void_p), a.nbytes))
+        return self
+
+    def export(self):
+        a = np.zeros(self._host_shape(), dtype=real_dtype(self.prec))
+        _chk(load().mesh_field_export(self.h, a.ctypes.data_as(C.c_void_p), a.nbytes))
+        return a if self.nstack > 1 else a[0]
+
+    def copy_from(self, other: "Field"):
+        _chk(load().mesh_field_copy(self.h, other.h))
+        return self
+
+    def set_zero(self):
+        _chk(load().mesh_field_set_zero(self.h))
+        return self
+
+    def set_unit(self):
+        _chk(load().mesh_field_set_unit(self.h))
+        return self
+
+    def random(self, seed: int, counter: int = 0):
+        _chk(load().mesh_field_random(self.h, seed, counter))
+        return self
+
+    def norm2(self) -> float:
+        out = C.c_double()
+        _chk(load().mesh_field_norm2(self.h, C.byref(out)))
+        return out.value
+
+    @property
+    def device_ptr(self) -> int:
+        return load().mesh_field_device_ptr(self.h) or 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mesh_field_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def GaugeField(ctx, group, prec, grid) -> Field:
+    """GaugeField<G> = LatticeStack<G> (utils.h:21): nd link components."""
+    return Field(ctx, GROUP, group, prec, grid, grid.ndim)
+
+
+def Momenta(ctx, group, prec, grid) -> Field:
+    """Conjugate momenta: nd algebra components."""
+    return Field(ctx, ALGEBRA, group, prec, grid, grid.ndim)
+
+
+def Lattice(ctx, group, prec, grid, algebra: bool = False) -> Field:
+    """Lattice<G> (lattice.h:23-143): one object per site."""
+    return Field(ctx, ALGEBRA if algebra else GROUP, group, prec, grid, 1)
+
+
+# ---- lattice layer ----------------------------------------------------------
+def cshift(dst: Field, src: Field, dir: int, offset: int) -> Field:
+    _chk(load().mesh_site_cshift(dst.h, src.h, dir, offset))
+    return dst
+
+
+def site_mul(dst: Field, a: Field, b: Field) -> Field:
+    _chk(load().mesh_site_mul(dst.h, a.h, b.h))
+    return dst
+
+
+def site_adj(dst: Field, a: Field) -> Field:
+    _chk(load().mesh_site_adj(dst.h, a.h))
+    return dst
+
+
+def sum_real_trace(a: Field) -> float:
+    out = C.c_double()
+    _chk(load().mesh_site_sum_real_trace(a.h, C.byref(out)))
+    return out.value
+
+
+def norm2(a: Field) -> float:
+    return a.norm2()
+
+
+# ---- gauge ------------------------------------------------------------------
+def plaquette(U: Field) -> float:
+    out = C.c_double()
+    _chk(load().mesh_plaquette(U.h, C.byref(out)))
+    return out.value
+
+
+def wilson_action(U: Field, beta: float) -> float:
+    out = C.c_double()
+    _chk(load().mesh_wilson_action(U.h, beta, C.byref(out)))
+    return out.value
+
+
+def staple_sum(S: Field, U: Field, mu: int) -> Field:
+    _chk(load().mesh_staple_sum(S.h, U.h, mu))
+    return S
+
+
+def wilson_deriv(F: Field, U: Field, mu: int, beta: float) -> Field:
+    _chk(load().mesh_wilson_deriv(F.h, U.h, mu, beta))
+    return F
+
+
+def reunitize(U: Field) -> Field:
+    _chk(load().mesh_reunitize(U.h))
+    return U
+
+
+def evolve(U: Field, P: Field, t: float) -> Field:
+    _chk(load().mesh_evolve(U.h, P.h, t))
+    return U
+
+
+def momentum_step(P: Field, U: Field, beta: float, delta: float) -> Field:
+    _chk(load().mesh_momentum_step(P.h, U.h, beta, delta))
+    return P
+
+
+def run_hmd(U: Field, P: Field, beta: float, deltas) -> None:
+    a, p = _darr(deltas)
+    _chk(load().mesh_run_hmd(U.h, P.h, beta, p, len(a)))
+
+
+def make_deltas(scheme: str, epsilon: float, substeps: int) -> np.ndarray:
+    n = C.c_int()
+    cap = 8 * substeps + 16
+    buf = (C.c_double * cap)()
+    _chk(load().mesh_make_deltas(scheme.encode(), epsilon, substeps, buf, cap, C.byref(n)))
+    return np.array(buf[: n.value])
+
+
+def gauge_transform(U: Field, g: Field) -> Field:
+    _chk(load().mesh_gauge_transform(U.h, g.h))
+    return U
+
+
+# ---- HMC --------------------------------------------------------------------
+class Hmc:
+    """Hmc<G> (hmc.h:287-336): U, P, proposal, histories; momenta and the
+    Metropolis uniform from counter-based device streams keyed by `seed`."""
+
+    def __init__(self, ctx: Context, group, prec: int, grid: Grid, seed: int):
+        self.ctx, self.group, self.prec, self.grid = ctx, group_code(group), prec, grid
+        h = C.c_void_p()
+        _chk(load().mesh_hmc_create(ctx.h, self.group, prec, grid.ndim, _dims(grid.shape), seed, C.byref(h)))
+        self.h = h
+        self._U = self._borrow(0)
+        self._P = self._borrow(1)
+
+    def _borrow(self, which):
+        out = C.c_void_p()
+        _chk(load().mesh_hmc_field(self.h, which, C.byref(out)))
+        f = Field.__new__(Field)
+        f.ctx, f.kind, f.group, f.prec, f.grid = self.ctx, GROUP if which == 0 else ALGEBRA, self.group, self.prec, \
+            self.grid
+        f.nstack = self.grid.ndim
+        f.h = out
+        f.close = lambda: None  # borrowed: owned by the chain
+        return f
+
+    @property
+    def U(self) -> Field:
+        # writes through the handle invalidate the cached action
+        _chk(load().mesh_hmc_field(self.h, 0, C.byref(C.c_void_p())))
+        return self._U
+
+    @property
+    def P(self) -> Field:
+        return self._P
+
+    def randomize_gauge_field(self):
+        _chk(load().mesh_hmc_randomize(self.h))
+
+    def cold_start(self):
+        _chk(load().mesh_hmc_cold_start(self.h))
+
+    def update(self, beta: float, deltas) -> dict:
+        a, p = _darr(deltas)
+        rec = HmcRecord()
+        _chk(load().mesh_hmc_update(self.h, beta, p, len(a), C.byref(rec)))
+        return rec.as_dict()
+
+    def update_supplied(self, P0: Field, uniform: float, beta: float, deltas) -> dict:
+        a, p = _darr(deltas)
+        rec = HmcRecord()
+        _chk(load().mesh_hmc_update_supplied(self.h, P0.h, uniform, beta, p, len(a), C.byref(rec)))
+        return rec.as_dict()
+
+    def run(self, beta: float, deltas, count: int, use_graph: bool = True):
+        a, p = _darr(deltas)
+        _chk(load().mesh_hmc_run(self.h, beta, p, len(a), count, 1 if use_graph else 0))
+
+    def run_host(self, host_U: np.ndarray, beta: float, deltas, count: int = 1) -> dict:
+        a, p = _darr(deltas)
+        rec = HmcRecord()
+        assert host_U.flags["C_CONTIGUOUS"]
+        _chk(load().mesh_hmc_run_host(self.h, host_U.ctypes.data_as(C.c_void_p), host_U.nbytes, beta, p, len(a),
+                                      count, C.byref(rec)))
+        return rec.as_dict()
+
+    @property
+    def count(self) -> int:
+        n = C.c_int()
+        _chk(load().mesh_hmc_count(self.h, C.byref(n)))
+        return n.value
+
+    def history(self, first: int = 0, count: int | None = None):
+        if count is None:
+            count = self.count - first
+        pl, dh, ac = (np.zeros(count) for _ in range(3))
+        _chk(load().mesh_hmc_history(self.h, first, count, pl.ctypes.data_as(_DP), dh.ctypes.data_as(_DP),
+                                     ac.ctypes.data_as(_DP)))
+        return {"plaq_history": pl, "deltaH_history": dh, "accept_history": ac}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mesh_hmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- Landau -----------------------------------------------------------------
+class Landau:
+    """Landau<G> (landau.h:8-137): gauge transform g for fixed links U."""
+
+    def __init__(self, U: Field):
+        self.U = U
+        self.g = Lattice(U.ctx, U.group, U.prec, U.grid).set_unit()
+
+    def reset(self):
+        self.g.set_unit()
+
+    def __call__(self) -> float:
+        out = C.c_double()
+        _chk(load().mesh_landau_functional(self.U.h, self.g.h, C.byref(out)))
+        return out.value
+
+    def condition(self) -> float:
+        out = C.c_double()
+        _chk(load().mesh_landau_theta(self.U.h, self.g.h, C.byref(out)))
+        return out.value
+
+    def deriv(self) -> Field:
+        F = Lattice(self.U.ctx, self.U.group, self.U.prec, self.U.grid, algebra=True)
+        _chk(load().mesh_landau_deriv(F.h, self.U.h, self.g.h))
+        return F
+
+    def run(self, max_iter: int, tol: float = 1e-10, raise_on_noconv: bool = False):
+        it, th = C.c_int(), C.c_double()
+        rc = load().mesh_landau_cg(self.U.h, self.g.h, max_iter, tol, C.byref(it), C.byref(th))
+        if rc != 0 and (rc != 6 or raise_on_noconv):
+            _chk(rc)
+        return it.value, th.value
+
+    def overrelax(self, omega: float = 1.7, tol: float = 1e-12, max_sweeps: int = 100000, check_every: int = 10,
+                  raise_on_noconv: bool = False):
+        s, th = C.c_int(), C.c_double()
+        rc = load().mesh_landau_or(self.U.h, self.g.h, omega, tol, max_sweeps, check_every, C.byref(s), C.byref(th))
+        if rc != 0 and (rc != 6 or raise_on_noconv):
+            _chk(rc)
+        return s.value, th.value

@@ -1,0 +1,132 @@
+// Host-side objects behind the C ABI handles, and the per-(group, precision,
+// dimension) operation table that the C ABI dispatches through.
+#pragma once
+
+#include "common.cuh"
+#include "layout.cuh"
+#include "reduce.cuh"
+
+#include <vector>
+
+namespace meshgb {
+
+struct Field
+{
+	Context *ctx = nullptr;
+	int kind = MESH_GROUP; // MESH_GROUP / MESH_ALGEBRA
+	int group = 0, prec = 0, nd = 0, nstack = 0;
+	int32_t dims[4] = {0, 0, 0, 0};
+	Geom geom{};
+	int nr = 0;        // reals per object on the device
+	int nr_host = 0;   // reals per object on the host (full group type)
+	size_t real_bytes = 0;
+	void *d = nullptr; // device storage
+	size_t bytes = 0;
+
+	size_t host_bytes() const { return size_t(nstack) * size_t(geom.V) * size_t(nr_host) * real_bytes; }
+	bool same_grid(Field const &o) const
+	{
+		if (nd != o.nd || ctx != o.ctx)
+			return false;
+		for (int i = 0; i < nd; ++i)
+			if (dims[i] != o.dims[i])
+				return false;
+		return true;
+	}
+};
+
+inline int group_nr(int group) { return group == 1 ? 2 : group == 2 ? 4 : 18; }
+inline int group_na(int group) { return group == 1 ? 1 : group == 2 ? 3 : 8; }
+inline int group_nc(int group) { return group == 1 ? 1 : group == 2 ? 2 : 3; }
+
+inline RedSlot slot(Context &c, int k)
+{
+	return {c.d_partials + size_t(k) * kMaxRedBlocks, c.d_results + k, c.d_counters + k};
+}
+
+// device-resident HMC bookkeeping
+struct HmcDev
+{
+	uint64_t traj;   // trajectories done (momentum / Metropolis stream counter)
+	int accept_last; // decision of the last trajectory
+	int history_cap;
+	int bad;         // set when a Hamiltonian is not finite
+};
+struct HmcRecordDev
+{
+	double plaq, dH, accept, H_old, H_new;
+};
+
+// Kinds of element-wise site operations (lattice_apply layer)
+enum SiteOp
+{
+	SITE_MUL = 0,
+	SITE_ADJ = 1,
+	SITE_COPY = 2,
+};
+
+// Scalar-producing reduction slots (indices into the context's slots)
+enum SlotId
+{
+	SLOT_TMP = 0,
+	SLOT_TMP2 = 1,
+};
+
+struct OpsTable
+{
+	// fields
+	void (*import_)(Field &f, void const *d_stage);
+	void (*export_)(Field const &f, void *d_stage);
+	void (*set_unit)(Field &f);
+	void (*random)(Field &f, uint64_t seed, uint64_t counter, RedSlot kin);
+	// momenta from the stream counter held on the device (HMC refresh)
+	void (*random_momenta_dev)(Field &P, uint64_t seed, uint64_t const *counter_dev, RedSlot kin);
+	void (*norm2)(Field const &f, RedSlot out);
+	// lattice layer on single-component group fields
+	void (*cshift)(Field &dst, Field const &src, int dir, int offset);
+	void (*site_op)(int op, Field &dst, Field const &a, Field const *b);
+	void (*sum_real_trace)(Field const &a, RedSlot out);
+	// gauge
+	void (*plaquette)(Field const &U, RedSlot out);
+	void (*staple_sum)(Field &S, Field const &U, int mu);
+	void (*wilson_deriv)(Field &F, Field const &U, int mu, double beta);
+	void (*reunitize)(Field &U);
+	void (*evolve)(Field const &Usrc, Field &Udst, Field const &P, double t, bool reunit);
+	void (*momentum_step)(Field &P, Field const &U, double coef, RedSlot *kin);
+	// Landau
+	void (*landau_functional)(Field const &U, Field const &g, RedSlot out);
+	void (*landau_theta)(Field const &U, Field const &g, RedSlot out);
+	void (*landau_deriv)(Field &F, Field const &U, Field const &g, double scale);
+	void (*landau_or_half)(Field const &U, Field &g, double omega, int parity);
+	void (*reunit_exact)(Field &g);
+	void (*alg_dot)(Field const &a, Field const &b, RedSlot out);
+	void (*exp_apply)(Field &dst, Field const &F, double eps, Field const &g);
+	void (*axpy_alg)(Field &y, double a, Field const &x);
+	void (*gauge_transform)(Field &U, Field const &g);
+};
+
+OpsTable const *ops_u1(int prec, int nd);
+OpsTable const *ops_su2(int prec, int nd);
+OpsTable const *ops_su3(int prec, int nd);
+
+inline OpsTable const &ops_for(int group, int prec, int nd)
+{
+	OpsTable const *t = nullptr;
+	if (group == 1)
+		t = ops_u1(prec, nd);
+	else if (group == 2)
+		t = ops_su2(prec, nd);
+	else if (group == 3)
+		t = ops_su3(prec, nd);
+	require(t != nullptr, "unsupported (group, precision, dimension) combination");
+	return *t;
+}
+inline OpsTable const &ops_for(Field const &f) { return ops_for(f.group, f.prec, f.nd); }
+
+// HMC trajectory kernels (hmc.cu)
+void launch_metropolis(Context &c, HmcDev *dev, HmcRecordDev *hist, double const *S_cur, double const *K_old,
+                       double const *S_new, double const *K_new, double *S_cur_out, double beta, double nplanes_V,
+                       double Nc, uint64_t seed, double uniform, int *accept_flag);
+void launch_copy_if(Context &c, void *dst, void const *src, size_t bytes, int const *flag);
+
+} // namespace meshgb

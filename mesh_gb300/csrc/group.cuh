@@ -1,0 +1,581 @@
+// Per-element group and algebra arithmetic for U(1), SU(2), SU(3) in float or
+// double, for device (and host) code.
+//
+// Element layouts are the reference's object layouts (src/gauge/groups.h):
+//   U(1):  complex      (re, im)                       2 reals
+//   SU(2): quaternion   (re, im1, im2, im3)            4 reals, Hamilton product
+//   SU(3): 3x3 complex  row-major (re, im) pairs      18 reals
+// Algebra elements (momenta, forces) are stored packed:
+//   U(1): 1 real a <-> (0, a);  SU(2): 3 reals <-> (0, v1, v2, v3);
+//   SU(3): 8 reals (a0, a1, b01, b02, b12) <->
+//          [[i a0, b01, b02], [-b01*, i a1, b12], [-b02*, -b12*, -i(a0+a1)]].
+//
+// Operations follow groups.h: adj (:55,135,214), real_trace (:59,137,219),
+// project_on_algebra (:64,142,224), project_on_group_fast (:79,188,237),
+// exp (:103,153,263). The SU(3) exponential of an algebra element uses the
+// Cayley-Hamilton form exp(iQ) = f0 + f1 Q + f2 Q^2 of Morningstar & Peardon,
+// Phys. Rev. D 69 (2004) 054501, eqs. (19)-(35), instead of util::exp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#ifndef MESH_HD
+#define MESH_HD __host__ __device__ __forceinline__
+#endif
+
+namespace meshgb {
+
+template <class T> struct cx
+{
+	T re, im;
+};
+template <class T> MESH_HD cx<T> cmul(cx<T> a, cx<T> b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+template <class T> MESH_HD cx<T> cadd(cx<T> a, cx<T> b) { return {a.re + b.re, a.im + b.im}; }
+template <class T> MESH_HD cx<T> csub(cx<T> a, cx<T> b) { return {a.re - b.re, a.im - b.im}; }
+template <class T> MESH_HD cx<T> cconj(cx<T> a) { return {a.re, -a.im}; }
+template <class T> MESH_HD cx<T> cscale(cx<T> a, T s) { return {a.re * s, a.im * s}; }
+
+template <class T> MESH_HD T m_sqrt(T x) { return sqrt(x); }
+template <class T> MESH_HD T m_rsqrt(T x) { return T(1) / sqrt(x); }
+template <class T> MESH_HD void m_sincos(T x, T *s, T *c)
+{
+	*s = sin(x);
+	*c = cos(x);
+}
+#ifdef __CUDA_ARCH__
+template <> __device__ __forceinline__ void m_sincos<float>(float x, float *s, float *c) { sincosf(x, s, c); }
+template <> __device__ __forceinline__ void m_sincos<double>(double x, double *s, double *c) { sincos(x, s, c); }
+#endif
+
+enum
+{
+	U1 = 1,
+	SU2 = 2,
+	SU3 = 3
+};
+
+template <int GRP, class T> struct Group;
+
+// ---------------------------------------------------------------------------
+// U(1)
+// ---------------------------------------------------------------------------
+template <class T> struct Group<U1, T>
+{
+	using real = T;
+	static constexpr int NR = 2, NA = 1, NC = 1, DIM = 1;
+	static constexpr int NNORM_GROUP = 2; // normals for a Haar element
+	struct E
+	{
+		T v[2];
+	};
+	MESH_HD static E unit() { return {{T(1), T(0)}}; }
+	MESH_HD static E zero() { return {{T(0), T(0)}}; }
+	MESH_HD static E mul(E a, E b) { return {{a.v[0] * b.v[0] - a.v[1] * b.v[1], a.v[0] * b.v[1] + a.v[1] * b.v[0]}}; }
+	// a * b^dagger
+	MESH_HD static E mul_nd(E a, E b) { return {{a.v[0] * b.v[0] + a.v[1] * b.v[1], a.v[1] * b.v[0] - a.v[0] * b.v[1]}}; }
+	// a^dagger * b
+	MESH_HD static E mul_dn(E a, E b) { return {{a.v[0] * b.v[0] + a.v[1] * b.v[1], a.v[0] * b.v[1] - a.v[1] * b.v[0]}}; }
+	MESH_HD static E adj(E a) { return {{a.v[0], -a.v[1]}}; }
+	MESH_HD static void add_to(E &a, E b)
+	{
+		a.v[0] += b.v[0];
+		a.v[1] += b.v[1];
+	}
+	MESH_HD static void sub_from(E &a, E b)
+	{
+		a.v[0] -= b.v[0];
+		a.v[1] -= b.v[1];
+	}
+	MESH_HD static T retr(E a) { return a.v[0]; }
+	// ReTr(a b^dagger)
+	MESH_HD static T retr_nd(E a, E b) { return a.v[0] * b.v[0] + a.v[1] * b.v[1]; }
+	MESH_HD static void proj(E a, T *o) { o[0] = a.v[1]; }
+	MESH_HD static E from_alg(T const *o) { return {{T(0), o[0]}}; }
+	MESH_HD static T kin(T const *o) { return o[0] * o[0]; }
+	// exp(t X)
+	MESH_HD static E exp_alg(T const *o, T t)
+	{
+		T s, c;
+		m_sincos(o[0] * t, &s, &c);
+		return {{c, s}};
+	}
+	MESH_HD static E reunit_fast(E a)
+	{
+		T f = T(1.5) - (a.v[0] * a.v[0] + a.v[1] * a.v[1]) * T(0.5);
+		return {{a.v[0] * f, a.v[1] * f}};
+	}
+	MESH_HD static E reunit_exact(E a)
+	{
+		T f = m_rsqrt(a.v[0] * a.v[0] + a.v[1] * a.v[1]);
+		return {{a.v[0] * f, a.v[1] * f}};
+	}
+	MESH_HD static void alg_from_normals(T const *p, T *o) { o[0] = p[0] * T(0.70710678118654752440); }
+	MESH_HD static E group_from_normals(T const *p)
+	{
+		T t = atan2(p[1], p[0]);
+		T s, c;
+		m_sincos(t, &s, &c);
+		return {{c, s}};
+	}
+};
+
+// ---------------------------------------------------------------------------
+// SU(2) as unit quaternions
+// ---------------------------------------------------------------------------
+template <class T> struct Group<SU2, T>
+{
+	using real = T;
+	static constexpr int NR = 4, NA = 3, NC = 2, DIM = 3;
+	static constexpr int NNORM_GROUP = 4;
+	struct E
+	{
+		T v[4];
+	};
+	MESH_HD static E unit() { return {{T(1), T(0), T(0), T(0)}}; }
+	MESH_HD static E zero() { return {{T(0), T(0), T(0), T(0)}}; }
+	MESH_HD static E mul(E a, E b)
+	{
+		return {{a.v[0] * b.v[0] - a.v[1] * b.v[1] - a.v[2] * b.v[2] - a.v[3] * b.v[3],
+		         a.v[0] * b.v[1] + a.v[1] * b.v[0] + a.v[2] * b.v[3] - a.v[3] * b.v[2],
+		         a.v[0] * b.v[2] - a.v[1] * b.v[3] + a.v[2] * b.v[0] + a.v[3] * b.v[1],
+		         a.v[0] * b.v[3] + a.v[1] * b.v[2] - a.v[2] * b.v[1] + a.v[3] * b.v[0]}};
+	}
+	MESH_HD static E adj(E a) { return {{a.v[0], -a.v[1], -a.v[2], -a.v[3]}}; }
+	MESH_HD static E mul_nd(E a, E b) { return mul(a, adj(b)); }
+	MESH_HD static E mul_dn(E a, E b) { return mul(adj(a), b); }
+	MESH_HD static void add_to(E &a, E b)
+	{
+#pragma unroll
+		for (int i = 0; i < 4; ++i)
+			a.v[i] += b.v[i];
+	}
+	MESH_HD static void sub_from(E &a, E b)
+	{
+#pragma unroll
+		for (int i = 0; i < 4; ++i)
+			a.v[i] -= b.v[i];
+	}
+	MESH_HD static T retr(E a) { return a.v[0] * T(2); }
+	// ReTr(a b^dagger) = 2 Re(a conj(b)) = 2 a.b
+	MESH_HD static T retr_nd(E a, E b)
+	{
+		return T(2) * (a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2] + a.v[3] * b.v[3]);
+	}
+	MESH_HD static void proj(E a, T *o)
+	{
+		o[0] = a.v[1];
+		o[1] = a.v[2];
+		o[2] = a.v[3];
+	}
+	MESH_HD static E from_alg(T const *o) { return {{T(0), o[0], o[1], o[2]}}; }
+	// 2x2 Frobenius norm of the algebra element
+	MESH_HD static T kin(T const *o) { return T(2) * (o[0] * o[0] + o[1] * o[1] + o[2] * o[2]); }
+	MESH_HD static E exp_alg(T const *o, T t)
+	{
+		T a1 = o[0] * t, a2 = o[1] * t, a3 = o[2] * t;
+		T al = m_sqrt(a1 * a1 + a2 * a2 + a3 * a3);
+		T s, c;
+		m_sincos(al, &s, &c);
+		// sin(al)/al with its limit 1 at al == 0 (groups.h:153-164 divides)
+		T f = al == T(0) ? T(1) : s / al;
+		return {{c, a1 * f, a2 * f, a3 * f}};
+	}
+	MESH_HD static E reunit_fast(E a)
+	{
+		T n = a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2] + a.v[3] * a.v[3];
+		T f = T(1.5) - n * T(0.5);
+		return {{a.v[0] * f, a.v[1] * f, a.v[2] * f, a.v[3] * f}};
+	}
+	MESH_HD static E reunit_exact(E a)
+	{
+		T f = m_rsqrt(a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2] + a.v[3] * a.v[3]);
+		return {{a.v[0] * f, a.v[1] * f, a.v[2] * f, a.v[3] * f}};
+	}
+	MESH_HD static void alg_from_normals(T const *p, T *o)
+	{
+		o[0] = T(0.5) * p[0];
+		o[1] = T(0.5) * p[1];
+		o[2] = T(0.5) * p[2];
+	}
+	MESH_HD static E group_from_normals(T const *p) { return reunit_exact({{p[0], p[1], p[2], p[3]}}); }
+};
+
+// ---------------------------------------------------------------------------
+// SU(3) as 3x3 complex matrices
+// ---------------------------------------------------------------------------
+template <class T> struct Group<SU3, T>
+{
+	using real = T;
+	static constexpr int NR = 18, NA = 8, NC = 3, DIM = 8;
+	static constexpr int NNORM_GROUP = 18;
+	struct E
+	{
+		T v[18];
+		MESH_HD cx<T> at(int i, int j) const { return {v[6 * i + 2 * j], v[6 * i + 2 * j + 1]}; }
+		MESH_HD void set(int i, int j, cx<T> z)
+		{
+			v[6 * i + 2 * j] = z.re;
+			v[6 * i + 2 * j + 1] = z.im;
+		}
+	};
+	MESH_HD static E zero()
+	{
+		E r;
+#pragma unroll
+		for (int k = 0; k < 18; ++k)
+			r.v[k] = T(0);
+		return r;
+	}
+	MESH_HD static E unit()
+	{
+		E r = zero();
+		r.v[0] = r.v[8] = r.v[16] = T(1);
+		return r;
+	}
+	// c = a * b
+	MESH_HD static E mul(E const &a, E const &b)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				T re = a.v[6 * i] * b.v[2 * j] - a.v[6 * i + 1] * b.v[2 * j + 1];
+				T im = a.v[6 * i] * b.v[2 * j + 1] + a.v[6 * i + 1] * b.v[2 * j];
+#pragma unroll
+				for (int k = 1; k < 3; ++k)
+				{
+					re += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * j] - a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * j + 1];
+					im += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * j + 1] + a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * j];
+				}
+				r.v[6 * i + 2 * j] = re;
+				r.v[6 * i + 2 * j + 1] = im;
+			}
+		return r;
+	}
+	// c = a * b^dagger:  c_ij = sum_k a_ik conj(b_jk)
+	MESH_HD static E mul_nd(E const &a, E const &b)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				T re = 0, im = 0;
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+				{
+					T ar = a.v[6 * i + 2 * k], ai = a.v[6 * i + 2 * k + 1];
+					T br = b.v[6 * j + 2 * k], bi = b.v[6 * j + 2 * k + 1];
+					re += ar * br + ai * bi;
+					im += ai * br - ar * bi;
+				}
+				r.v[6 * i + 2 * j] = re;
+				r.v[6 * i + 2 * j + 1] = im;
+			}
+		return r;
+	}
+	// c = a^dagger * b:  c_ij = sum_k conj(a_ki) b_kj
+	MESH_HD static E mul_dn(E const &a, E const &b)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				T re = 0, im = 0;
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+				{
+					T ar = a.v[6 * k + 2 * i], ai = a.v[6 * k + 2 * i + 1];
+					T br = b.v[6 * k + 2 * j], bi = b.v[6 * k + 2 * j + 1];
+					re += ar * br + ai * bi;
+					im += ar * bi - ai * br;
+				}
+				r.v[6 * i + 2 * j] = re;
+				r.v[6 * i + 2 * j + 1] = im;
+			}
+		return r;
+	}
+	MESH_HD static E adj(E const &a)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				r.v[6 * i + 2 * j] = a.v[6 * j + 2 * i];
+				r.v[6 * i + 2 * j + 1] = -a.v[6 * j + 2 * i + 1];
+			}
+		return r;
+	}
+	MESH_HD static void add_to(E &a, E const &b)
+	{
+#pragma unroll
+		for (int k = 0; k < 18; ++k)
+			a.v[k] += b.v[k];
+	}
+	MESH_HD static void sub_from(E &a, E const &b)
+	{
+#pragma unroll
+		for (int k = 0; k < 18; ++k)
+			a.v[k] -= b.v[k];
+	}
+	MESH_HD static T retr(E const &a) { return a.v[0] + a.v[8] + a.v[16]; }
+	MESH_HD static T retr_nd(E const &a, E const &b)
+	{
+		T s = 0;
+#pragma unroll
+		for (int k = 0; k < 18; ++k)
+			s += a.v[k] * b.v[k];
+		return s;
+	}
+	// antihermitian traceless part, packed
+	MESH_HD static void proj(E const &a, T *o)
+	{
+		T t = (a.v[1] + a.v[9] + a.v[17]) * T(1.0 / 3.0);
+		o[0] = a.v[1] - t;
+		o[1] = a.v[9] - t;
+		o[2] = (a.v[2] - a.v[6]) * T(0.5);
+		o[3] = (a.v[3] + a.v[7]) * T(0.5);
+		o[4] = (a.v[4] - a.v[12]) * T(0.5);
+		o[5] = (a.v[5] + a.v[13]) * T(0.5);
+		o[6] = (a.v[10] - a.v[14]) * T(0.5);
+		o[7] = (a.v[11] + a.v[15]) * T(0.5);
+	}
+	MESH_HD static E from_alg(T const *o)
+	{
+		E r;
+		r.v[0] = 0;
+		r.v[1] = o[0];
+		r.v[8] = 0;
+		r.v[9] = o[1];
+		r.v[16] = 0;
+		r.v[17] = -(o[0] + o[1]);
+		r.v[2] = o[2];
+		r.v[3] = o[3];
+		r.v[4] = o[4];
+		r.v[5] = o[5];
+		r.v[10] = o[6];
+		r.v[11] = o[7];
+		r.v[6] = -o[2];
+		r.v[7] = o[3];
+		r.v[12] = -o[4];
+		r.v[13] = o[5];
+		r.v[14] = -o[6];
+		r.v[15] = o[7];
+		return r;
+	}
+	// sum_ij |A_ij|^2 of the algebra element
+	MESH_HD static T kin(T const *o)
+	{
+		T d = o[0] + o[1];
+		return o[0] * o[0] + o[1] * o[1] + d * d +
+		       T(2) * (o[2] * o[2] + o[3] * o[3] + o[4] * o[4] + o[5] * o[5] + o[6] * o[6] + o[7] * o[7]);
+	}
+	MESH_HD static cx<T> det(E const &m)
+	{
+		cx<T> a = cmul(m.at(1, 1), m.at(2, 2)), b = cmul(m.at(1, 2), m.at(2, 1));
+		cx<T> c = cmul(m.at(1, 0), m.at(2, 2)), d = cmul(m.at(1, 2), m.at(2, 0));
+		cx<T> e = cmul(m.at(1, 0), m.at(2, 1)), f = cmul(m.at(1, 1), m.at(2, 0));
+		cx<T> r = cmul(m.at(0, 0), csub(a, b));
+		r = csub(r, cmul(m.at(0, 1), csub(c, d)));
+		return cadd(r, cmul(m.at(0, 2), csub(e, f)));
+	}
+	// exp(t X) for X = from_alg(o) (antihermitian traceless), Cayley-Hamilton
+	MESH_HD static E exp_alg(T const *o, T t)
+	{
+		T x[8];
+#pragma unroll
+		for (int k = 0; k < 8; ++k)
+			x[k] = o[k] * t;
+		E X = from_alg(x);
+		E X2 = mul(X, X);
+		// c1 = Tr(Q^2)/2 = |X|^2/2,  c0 = det(Q) = det(-iX) = -Im det(X)
+		T c1 = T(0.5) * kin(x);
+		T c0 = -det(X).im;
+		cx<T> f0, f1, f2;
+		T const tiny = sizeof(T) == 8 ? T(1e-11) : T(1e-5);
+		if (c1 < tiny)
+		{
+			// exp(X) = 1 + X + X^2/2 + X^3/6; with X^3 = -i Q^3 and
+			// Q^3 = c1 Q + c0: 1 + X + X^2/2 - i (c1 Q + c0)/6
+			// -> f0 = 1 - i c0/6, f1 (on Q) = i - i c1/6, f2 (on Q^2) = -1/2
+			f0 = {T(1), -c0 * T(1.0 / 6.0)};
+			f1 = {T(0), T(1) - c1 * T(1.0 / 6.0)};
+			f2 = {T(-0.5), T(0)};
+		}
+		else
+		{
+			bool neg = c0 < T(0);
+			T c0a = neg ? -c0 : c0;
+			T sq = m_sqrt(c1 * T(1.0 / 3.0));
+			T c0max = T(2) * sq * sq * sq;
+			T ratio = c0a / c0max;
+			ratio = ratio > T(1) ? T(1) : ratio;
+			T theta = acos(ratio);
+			T st, ct;
+			m_sincos(theta * T(1.0 / 3.0), &st, &ct);
+			T u = sq * ct;
+			T w = m_sqrt(c1) * st;
+			T u2 = u * u, w2 = w * w;
+			T s2u, c2u, su, cu, sw, cw;
+			m_sincos(T(2) * u, &s2u, &c2u);
+			m_sincos(u, &su, &cu);
+			m_sincos(w, &sw, &cw);
+			T xi0;
+			if (w < T(0.05))
+				xi0 = T(1) - w2 * T(1.0 / 6.0) * (T(1) - w2 * T(1.0 / 20.0) * (T(1) - w2 * T(1.0 / 42.0)));
+			else
+				xi0 = sw / w;
+			cx<T> e2iu = {c2u, s2u};
+			cx<T> emiu = {cu, -su};
+			// h0 = (u^2 - w^2) e^{2iu} + e^{-iu} [8u^2 cos w + 2iu(3u^2 + w^2) xi0]
+			cx<T> h0 = cadd(cscale(e2iu, u2 - w2),
+			                cmul(emiu, cx<T>{T(8) * u2 * cw, T(2) * u * (T(3) * u2 + w2) * xi0}));
+			// h1 = 2u e^{2iu} - e^{-iu} [2u cos w - i(3u^2 - w^2) xi0]
+			cx<T> h1 = csub(cscale(e2iu, T(2) * u), cmul(emiu, cx<T>{T(2) * u * cw, -(T(3) * u2 - w2) * xi0}));
+			// h2 = e^{2iu} - e^{-iu} [cos w + 3iu xi0]
+			cx<T> h2 = csub(e2iu, cmul(emiu, cx<T>{cw, T(3) * u * xi0}));
+			T inv = T(1) / (T(9) * u2 - w2);
+			f0 = cscale(h0, inv);
+			f1 = cscale(h1, inv);
+			f2 = cscale(h2, inv);
+			if (neg)
+			{
+				// f_j(-c0) = (-1)^j conj(f_j(c0))
+				f0 = cconj(f0);
+				f1 = {-f1.re, f1.im};
+				f2 = cconj(f2);
+			}
+		}
+		// exp(iQ) = f0 + f1 Q + f2 Q^2 with Q = -iX, Q^2 = -X^2:
+		//         = f0 - i f1 X - f2 X^2
+		cx<T> g1 = {f1.im, -f1.re}; // -i f1
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				cx<T> z = csub(cmul(g1, X.at(i, j)), cmul(f2, X2.at(i, j)));
+				if (i == j)
+					z = cadd(z, f0);
+				r.set(i, j, z);
+			}
+		return r;
+	}
+	// project_on_group_fast (groups.h:237-243):
+	// r = 1.5 a - 0.5 a a^dagger a;  r (4/3 - det(r)/3)
+	MESH_HD static E reunit_fast(E const &a)
+	{
+		E aa = mul_nd(a, a);
+		E aaa = mul(aa, a);
+		E r;
+#pragma unroll
+		for (int k = 0; k < 18; ++k)
+			r.v[k] = a.v[k] * T(1.5) - aaa.v[k] * T(0.5);
+		cx<T> d = det(r);
+		cx<T> f = {T(4.0 / 3.0) - d.re * T(1.0 / 3.0), -d.im * T(1.0 / 3.0)};
+		E o;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+				o.set(i, j, cmul(r.at(i, j), f));
+		return o;
+	}
+	// exact: Gram-Schmidt rows 0,1; row 2 = conj(row0 x row1)
+	MESH_HD static E reunit_exact(E const &a)
+	{
+		E r;
+		T n0 = 0;
+#pragma unroll
+		for (int k = 0; k < 6; ++k)
+			n0 += a.v[k] * a.v[k];
+		n0 = m_rsqrt(n0);
+#pragma unroll
+		for (int k = 0; k < 6; ++k)
+			r.v[k] = a.v[k] * n0;
+		cx<T> ip = {T(0), T(0)};
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+			ip = cadd(ip, cmul(cconj(r.at(0, j)), a.at(1, j)));
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+			r.set(1, j, csub(a.at(1, j), cmul(r.at(0, j), ip)));
+		T n1 = 0;
+#pragma unroll
+		for (int k = 6; k < 12; ++k)
+			n1 += r.v[k] * r.v[k];
+		n1 = m_rsqrt(n1);
+#pragma unroll
+		for (int k = 6; k < 12; ++k)
+			r.v[k] *= n1;
+		r.set(2, 0, cconj(csub(cmul(r.at(0, 1), r.at(1, 2)), cmul(r.at(0, 2), r.at(1, 1)))));
+		r.set(2, 1, cconj(csub(cmul(r.at(0, 2), r.at(1, 0)), cmul(r.at(0, 0), r.at(1, 2)))));
+		r.set(2, 2, cconj(csub(cmul(r.at(0, 0), r.at(1, 1)), cmul(r.at(0, 1), r.at(1, 0)))));
+		return r;
+	}
+	// Gaussian algebra element: i/2 sum_a p_a lambda_a (Gell-Mann)
+	MESH_HD static void alg_from_normals(T const *p, T *o)
+	{
+		T const r3 = T(0.57735026918962576451);
+		o[0] = T(0.5) * (p[2] + p[7] * r3);
+		o[1] = T(0.5) * (-p[2] + p[7] * r3);
+		o[2] = T(0.5) * p[1];
+		o[3] = T(0.5) * p[0];
+		o[4] = T(0.5) * p[4];
+		o[5] = T(0.5) * p[3];
+		o[6] = T(0.5) * p[6];
+		o[7] = T(0.5) * p[5];
+	}
+	// Haar element: Gram-Schmidt of a complex normal matrix, row 0 divided
+	// by the determinant (groups.h:255-261)
+	MESH_HD static E group_from_normals(T const *p)
+	{
+		E r;
+#pragma unroll
+		for (int k = 0; k < 18; ++k)
+			r.v[k] = p[k];
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+#pragma unroll
+			for (int k = 0; k < i; ++k)
+			{
+				cx<T> ip = {T(0), T(0)};
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+					ip = cadd(ip, cmul(cconj(r.at(k, j)), r.at(i, j)));
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+					r.set(i, j, csub(r.at(i, j), cmul(r.at(k, j), ip)));
+			}
+			T n = 0;
+#pragma unroll
+			for (int j = 0; j < 6; ++j)
+				n += r.v[6 * i + j] * r.v[6 * i + j];
+			n = T(1) / m_sqrt(n);
+#pragma unroll
+			for (int j = 0; j < 6; ++j)
+				r.v[6 * i + j] *= n;
+		}
+		cx<T> d = det(r);
+		T dn = T(1) / (d.re * d.re + d.im * d.im);
+		cx<T> inv = {d.re * dn, -d.im * dn};
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+			r.set(0, j, cmul(r.at(0, j), inv));
+		return r;
+	}
+};
+
+} // namespace meshgb

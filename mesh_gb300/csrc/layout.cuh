@@ -1,0 +1,231 @@
+// Device data layout: even/odd (checkerboard) site order, structure-of-arrays
+// planes read and written with 128-bit coalesced accesses.
+//
+// Site order. The reference indexes sites lexicographically with dimension 0
+// slowest (src/lattice/grid.h:39-49): r = (((x0 L1 + x1) L2 + x2) L3 + x3).
+// The device order puts all even sites (sum of coordinates even) first, then
+// all odd sites, each parity in lexicographic order:
+//     eo(r) = parity(r) * V/2 + floor(r / 2).
+// This is a bijection when the last extent is even (sites 2k and 2k+1 differ
+// in parity); every extent must be even for the checkerboard to be a proper
+// two-colouring under periodic wrap-around, which the library requires.
+//
+// Field storage. A field holds `nstack` components (the directions mu of a
+// gauge field) of V objects of NR reals. Component c occupies NR*V reals at
+// offset c*NR*V; inside it the NR reals of every site are split into planes:
+// float: floor(NR/4) float4 planes, then a float2 plane if NR%4 >= 2, then a
+// float plane if NR is odd; double: floor(NR/2) double2 planes, then a double
+// plane if NR is odd. Plane p of site s sits at plane_base + s, so a warp's
+// 32 consecutive sites read 32 consecutive 16-byte words.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace meshgb {
+
+struct Geom
+{
+	int nd;
+	int L[4];
+	int64_t V, Vh;
+	int64_t stride[4]; // lexicographic stride of dimension i
+};
+
+inline Geom make_geom(int nd, int32_t const *dims)
+{
+	Geom g{};
+	g.nd = nd;
+	g.V = 1;
+	for (int i = 0; i < 4; ++i)
+		g.L[i] = i < nd ? dims[i] : 1;
+	for (int i = nd - 1; i >= 0; --i)
+	{
+		g.stride[i] = g.V;
+		g.V *= g.L[i];
+	}
+	for (int i = nd; i < 4; ++i)
+		g.stride[i] = 0;
+	g.Vh = g.V / 2;
+	return g;
+}
+
+// Coordinates, lexicographic index and parity of the site with even/odd
+// index s.
+template <int ND> struct Site
+{
+	int x[ND];
+	int64_t lex;
+	int par;
+};
+
+template <int ND> __device__ __forceinline__ Site<ND> site_from_eo(Geom const &g, int64_t s)
+{
+	Site<ND> st;
+	int p = s >= g.Vh ? 1 : 0;
+	// V < 2^31 is enforced at field creation: 32-bit division suffices
+	uint32_t r = uint32_t(s - p * g.Vh) * 2u;
+	int sum = 0;
+#pragma unroll
+	for (int i = ND - 1; i >= 0; --i)
+	{
+		uint32_t L = uint32_t(g.L[i]);
+		uint32_t q = r / L;
+		st.x[i] = int(r - q * L);
+		r = q;
+		sum += st.x[i];
+	}
+	int64_t lex = (s - p * g.Vh) * 2;
+	if ((sum & 1) != p)
+	{
+		st.x[ND - 1] += 1;
+		lex += 1;
+	}
+	st.lex = lex;
+	st.par = p;
+	return st;
+}
+
+// even/odd index of the neighbour site at x + d (d a small signed offset
+// vector given as (dir, sign) pairs). Single-step neighbour:
+template <int ND>
+__device__ __forceinline__ int64_t eo_shift1(Geom const &g, Site<ND> const &st, int dir, int sign)
+{
+	int xd = st.x[dir] + sign;
+	int64_t lex = st.lex;
+	if (xd == g.L[dir])
+		lex -= int64_t(g.L[dir] - 1) * g.stride[dir];
+	else if (xd < 0)
+		lex += int64_t(g.L[dir] - 1) * g.stride[dir];
+	else
+		lex += sign * g.stride[dir];
+	return int64_t(st.par ^ 1) * g.Vh + (lex >> 1);
+}
+
+// neighbour at x + s1*e_d1 + s2*e_d2 (d1 != d2); same parity as x
+template <int ND>
+__device__ __forceinline__ int64_t eo_shift2(Geom const &g, Site<ND> const &st, int d1, int s1, int d2, int s2)
+{
+	int64_t lex = st.lex;
+	int a = st.x[d1] + s1;
+	if (a == g.L[d1])
+		lex -= int64_t(g.L[d1] - 1) * g.stride[d1];
+	else if (a < 0)
+		lex += int64_t(g.L[d1] - 1) * g.stride[d1];
+	else
+		lex += s1 * g.stride[d1];
+	int b = st.x[d2] + s2;
+	if (b == g.L[d2])
+		lex -= int64_t(g.L[d2] - 1) * g.stride[d2];
+	else if (b < 0)
+		lex += int64_t(g.L[d2] - 1) * g.stride[d2];
+	else
+		lex += s2 * g.stride[d2];
+	return int64_t(st.par) * g.Vh + (lex >> 1);
+}
+
+// host-side even/odd index of a lexicographic site (same formula)
+inline int64_t eo_index_host(Geom const &g, int64_t r)
+{
+	int64_t q = r;
+	int sum = 0;
+	for (int i = g.nd - 1; i >= 0; --i)
+	{
+		sum += int(q % g.L[i]);
+		q /= g.L[i];
+	}
+	return int64_t(sum & 1) * g.Vh + r / 2;
+}
+
+// ---------------------------------------------------------------------------
+// structure-of-arrays planes
+// ---------------------------------------------------------------------------
+template <class T, int NR> struct Soa;
+
+template <int NR> struct Soa<float, NR>
+{
+	static constexpr int N4 = NR / 4;
+	static constexpr int R = NR % 4;
+	__device__ __forceinline__ static void load(float const *__restrict__ base, int64_t V, int64_t s, float *v)
+	{
+		float4 const *p4 = reinterpret_cast<float4 const *>(base);
+#pragma unroll
+		for (int k = 0; k < N4; ++k)
+		{
+			float4 t = p4[k * V + s];
+			v[4 * k] = t.x;
+			v[4 * k + 1] = t.y;
+			v[4 * k + 2] = t.z;
+			v[4 * k + 3] = t.w;
+		}
+		float const *tail = base + int64_t(4 * N4) * V;
+		if constexpr (R >= 2)
+		{
+			float2 t = reinterpret_cast<float2 const *>(tail)[s];
+			v[4 * N4] = t.x;
+			v[4 * N4 + 1] = t.y;
+			tail += 2 * V;
+		}
+		if constexpr (R & 1)
+			v[NR - 1] = tail[s];
+	}
+	__device__ __forceinline__ static void store(float *__restrict__ base, int64_t V, int64_t s, float const *v)
+	{
+		float4 *p4 = reinterpret_cast<float4 *>(base);
+#pragma unroll
+		for (int k = 0; k < N4; ++k)
+			p4[k * V + s] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+		float *tail = base + int64_t(4 * N4) * V;
+		if constexpr (R >= 2)
+		{
+			reinterpret_cast<float2 *>(tail)[s] = make_float2(v[4 * N4], v[4 * N4 + 1]);
+			tail += 2 * V;
+		}
+		if constexpr (R & 1)
+			tail[s] = v[NR - 1];
+	}
+};
+
+template <int NR> struct Soa<double, NR>
+{
+	static constexpr int N2 = NR / 2;
+	__device__ __forceinline__ static void load(double const *__restrict__ base, int64_t V, int64_t s, double *v)
+	{
+		double2 const *p2 = reinterpret_cast<double2 const *>(base);
+#pragma unroll
+		for (int k = 0; k < N2; ++k)
+		{
+			double2 t = p2[k * V + s];
+			v[2 * k] = t.x;
+			v[2 * k + 1] = t.y;
+		}
+		if constexpr (NR & 1)
+			v[NR - 1] = (base + int64_t(2 * N2) * V)[s];
+	}
+	__device__ __forceinline__ static void store(double *__restrict__ base, int64_t V, int64_t s, double const *v)
+	{
+		double2 *p2 = reinterpret_cast<double2 *>(base);
+#pragma unroll
+		for (int k = 0; k < N2; ++k)
+			p2[k * V + s] = make_double2(v[2 * k], v[2 * k + 1]);
+		if constexpr (NR & 1)
+			(base + int64_t(2 * N2) * V)[s] = v[NR - 1];
+	}
+};
+
+// typed view of one component (direction) of a field
+template <class T, int NR> struct View
+{
+	T *base;
+	int64_t V;
+	__device__ __forceinline__ void load(int64_t s, T *v) const { Soa<T, NR>::load(base, V, s, v); }
+	__device__ __forceinline__ void store(int64_t s, T const *v) const { Soa<T, NR>::store(base, V, s, v); }
+};
+
+template <class T, int NR> __host__ __device__ __forceinline__ View<T, NR> comp(T *base, int64_t V, int c)
+{
+	return {base + int64_t(c) * NR * V, V};
+}
+
+} // namespace meshgb

@@ -602,3 +602,46 @@ int oracle_mlp_grad(int n, float const *x, float const *target, float const *par
 }
 
 } // extern "C"
+
+// ---- timing of the restated reference path (CPU baseline) ------------------
+// Times, on the host cores, one momentum step (P -= wilsonDeriv * delta for
+// all mu), one link update (evolve for all mu) and one plaquette of the
+// reference's algorithm on supplied fields; seconds per operation, best of
+// `reps`.
+#include <chrono>
+extern "C" int oracle_bench_md(int grp, int prec, int nd, int const *dims, void const *U, void const *P, double beta,
+                               double delta, int reps, double *t_force, double *t_evolve, double *t_plaq)
+{
+	return guarded([&] {
+		Grid g(nd, dims);
+		dispatch(grp, prec, [&](auto tag) {
+			using G = decltype(tag);
+			using clk = std::chrono::steady_clock;
+			auto u = load_stack<G>(g, nd, U);
+			auto p = load_stack<G>(g, nd, P);
+			double bf = 1e300, be = 1e300, bp = 1e300;
+			for (int r = 0; r < reps; ++r)
+			{
+				auto t0 = clk::now();
+				runHmd(g, u, p, beta, std::vector<double>{0.0, delta, 0.0});
+				auto t1 = clk::now();
+				// runHmd above also ran two evolve steps of length 0; time one
+				// evolve separately and subtract it twice
+				for (int mu = 0; mu < nd; ++mu)
+					evolve(u[mu], p[mu], delta);
+				auto t2 = clk::now();
+				double pl = plaquette(g, u);
+				auto t3 = clk::now();
+				(void)pl;
+				double te = std::chrono::duration<double>(t2 - t1).count();
+				double tf = std::chrono::duration<double>(t1 - t0).count() - 2 * te;
+				bf = std::min(bf, tf > 0 ? tf : std::chrono::duration<double>(t1 - t0).count());
+				be = std::min(be, te);
+				bp = std::min(bp, std::chrono::duration<double>(t3 - t2).count());
+			}
+			*t_force = bf;
+			*t_evolve = be;
+			*t_plaq = bp;
+		});
+	});
+}

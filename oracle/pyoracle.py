@@ -83,6 +83,7 @@ def lib():
             "oracle_landau_divergence": (I, [I, I, I, IP, P, P, P]),
             "oracle_fft": (I, [I, IP, I, DP, I]),
             "oracle_landau_fa_step": (I, [I, I, I, IP, P, P, DP, D]),
+            "oracle_bench_md": (I, [I, I, I, IP, P, P, D, D, I, DP, DP, DP]),
             "oracle_mlp_forward": (I, [I, C.POINTER(C.c_float), C.POINTER(C.c_float), I, C.POINTER(C.c_float)]),
             "oracle_mlp_grad": (I, [I, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), I, DP, DP]),
         }
@@ -437,3 +438,13 @@ def mlp_grad(x, t, params, width):
     _chk(lib().oracle_mlp_grad(x.shape[0], x.ctypes.data_as(fp), t.ctypes.data_as(fp), p.ctypes.data_as(fp),
                                width, C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_double))))
     return loss.value, g
+
+
+def bench_md(group, prec, dims, U, P, beta, delta, reps=1):
+    """Seconds per momentum step, link update and plaquette of the restated
+    reference algorithm on the host cores (best of reps)."""
+    nd, d = _dims(dims)
+    tf, te, tp = C.c_double(), C.c_double(), C.c_double()
+    _chk(lib().oracle_bench_md(group, prec, nd, d, _ptr(np.ascontiguousarray(U)), _ptr(np.ascontiguousarray(P)),
+                               beta, delta, reps, C.byref(tf), C.byref(te), C.byref(tp)))
+    return tf.value, te.value, tp.value

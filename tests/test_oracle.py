@@ -1,0 +1,146 @@
+"""CPU checks of the oracle: pinned against the reference's own templates
+(golden fixtures made by tests/golden/gen_golden.py from the reference code
+compiled in place, plus a live comparison where the reference tree is
+present), the Philox known-answer vectors, and the identities the reference's
+test prints (src/tests/lattice_gauge.cpp:23-40) turned into assertions."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(1e-300, float(np.max(np.abs(b)))))
+
+
+def test_philox_known_answers(oracle):
+    # Random123 known-answer vectors for philox4x32-10
+    assert oracle.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert oracle.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert oracle.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_matches_reference_golden(oracle, path):
+    z = np.load(path)
+    g, dims, beta = int(z["group"]), [int(x) for x in z["dims"]], float(z["beta"])
+    U, P = z["U"], z["P"]
+    nd = len(dims)
+    # FP64: the restatement reproduces the reference templates bit for bit
+    assert oracle.plaquette(g, 2, dims, U) == z["plaquette"]
+    assert oracle.wilson_action(g, 2, dims, U, beta) == z["action"]
+    np.testing.assert_array_equal(oracle.staple_sum(g, 2, dims, U, 1), z["staple_mu1"])
+    np.testing.assert_array_equal(oracle.wilson_deriv(g, 2, dims, U, 2 % nd, beta), z["deriv_mu2"])
+    np.testing.assert_array_equal(oracle.evolve(g, 2, dims, U, P, 0.1), z["evolve_t0p1"])
+    np.testing.assert_array_equal(oracle.reunitize(g, 2, dims, U * 1.0005), z["reunit"])
+    np.testing.assert_array_equal(oracle.cshift(g, 2, dims, np.ascontiguousarray(U[0]), 1, 1), z["cshift_d1_p1"])
+    np.testing.assert_array_equal(oracle.cshift(g, 2, dims, np.ascontiguousarray(U[1]), 0, -1), z["cshift_d0_m1"])
+    for sch in ("2lf", "2mn"):
+        d = oracle.make_deltas(sch, 0.5, 2)
+        np.testing.assert_array_equal(d, z[f"deltas_{sch}"])
+        Uo, Po = oracle.run_hmd(g, 2, dims, U, P, beta, d)
+        np.testing.assert_array_equal(Uo, z[f"hmd{sch}_U"])
+        np.testing.assert_array_equal(Po, z[f"hmd{sch}_P"])
+    np.testing.assert_array_equal(oracle.make_deltas("4mn", 1.0, 3), z["deltas_4mn"])
+    if "hmc_rec" in z.files:
+        Uh, r = oracle.hmc_update(g, 2, dims, U, P, beta, oracle.make_deltas("2lf", 0.5, 2), 0.25)
+        np.testing.assert_array_equal(Uh, z["hmc_U"])
+        assert [r["plaq"], r["dH"], r["accept"]] == list(z["hmc_rec"])
+
+
+def test_oracle_matches_reference_live(oracle):
+    """Same comparison against a fresh in-place build of the reference, on
+    other inputs and in FP32 too (skipped where the reference tree is absent)."""
+    import pyref
+
+    if not pyref.available():
+        pytest.skip("reference tree not present")
+    dims = [4, 2, 4, 6]
+    for g in (1, 2, 3):
+        for p, tol in ((2, 0.0), (1, 2e-6)):
+            U = oracle.random_gauge(g, p, dims, 31)
+            P = oracle.random_momenta(g, p, dims, 32, 0)
+            assert abs(oracle.plaquette(g, p, dims, U) - pyref.plaquette(g, p, dims, U)) <= tol
+            assert rel(oracle.wilson_deriv(g, p, dims, U, 3, 5.0), pyref.wilson_deriv(g, p, dims, U, 3, 5.0)) <= tol
+            d = oracle.make_deltas("2mn", 0.5, 2)
+            a, b = oracle.run_hmd(g, p, dims, U, P, 5.0, d), pyref.run_hmd(g, p, dims, U, P, 5.0, d)
+            assert rel(a[0], b[0]) <= 10 * tol and rel(a[1], b[1]) <= 10 * tol
+            if g != 2:
+                assert oracle.norm2(g, p, dims, P) == pytest.approx(pyref.norm2(g, p, dims, P), rel=max(tol, 1e-15))
+
+
+@pytest.mark.parametrize("g", [1, 2, 3])
+def test_reference_test_identities(oracle, g):
+    """src/tests/lattice_gauge.cpp:23-40: normalisation of random algebra
+    fields and the Landau finite-difference ratio, asserted."""
+    dims = [8, 8, 8, 8]
+    V, nd, dim = 8 ** 4, 4, {1: 1, 2: 3, 3: 8}[g]
+    P = oracle.random_momenta(g, 2, dims, 1234, 0)
+    r1 = oracle.norm2(g, 2, dims, P) / (V * nd * dim) / 0.5
+    s = sum(oracle.sum_real_trace(g, 2, dims, oracle.site_mul(g, 2, dims, P[mu], P[mu])) for mu in range(nd))
+    r2 = s / (V * nd * dim) / (-0.5)
+    assert abs(r1 - 1) < 5 / np.sqrt(V * nd * dim) * 3
+    assert r2 == pytest.approx(r1, rel=1e-12)
+    U = oracle.random_gauge(g, 2, dims, 7)
+    gt = oracle.unit_transform(g, 2, dims)
+    f = oracle.random_momenta(g, 2, dims, 99, 0)[0]
+    old = oracle.landau_functional(g, 2, dims, U, gt)
+    F = oracle.landau_deriv(g, 2, dims, U, gt)
+    eps = 1e-4
+    expected = -2 * eps * oracle.sum_real_trace(g, 2, dims, oracle.site_mul(g, 2, dims, f, F))
+    gn = oracle.evolve(g, 2, dims, np.stack([gt] * nd), np.stack([f] * nd), eps)[0]
+    assert (oracle.landau_functional(g, 2, dims, U, gn) - old) / expected == pytest.approx(1.0, abs=2e-3)
+
+
+@pytest.mark.parametrize("g,beta", [(2, 2.3), (3, 5.7)])
+def test_dH_scales_as_delta_squared(oracle, g, beta):
+    dims = [4, 4, 4, 4]
+    U = oracle.random_gauge(g, 2, dims, 7)
+    P = oracle.random_momenta(g, 2, dims, 11, 0)
+    dH = [oracle.hmc_update(g, 2, dims, U, P, beta, oracle.make_deltas("2lf", 0.5, n), 0.5)[1]["dH"]
+          for n in (10, 20, 40)]
+    assert dH[0] / dH[1] == pytest.approx(4.0, rel=0.05)
+    assert dH[1] / dH[2] == pytest.approx(4.0, rel=0.05)
+
+
+def test_reversibility_and_cold_start(oracle):
+    dims = [4, 4, 4, 4]
+    g = 3
+    U0 = oracle.unit_gauge(g, 2, dims)
+    assert oracle.plaquette(g, 2, dims, U0) == 1.0 and oracle.wilson_action(g, 2, dims, U0, 6.0) == 0.0
+    assert np.all(oracle.wilson_deriv(g, 2, dims, U0, 0, 6.0) == 0)
+    U = oracle.random_gauge(g, 2, dims, 3)
+    P = oracle.random_momenta(g, 2, dims, 4, 0)
+    d = oracle.make_deltas("2mn", 0.5, 4)
+    U1, P1 = oracle.run_hmd(g, 2, dims, U, P, 5.7, d)
+    U2, P2 = oracle.run_hmd(g, 2, dims, U1, -P1, 5.7, d)
+    assert rel(U2, U) < 1e-11 and rel(-P2, P) < 1e-11
+
+
+def test_gauge_invariance(oracle):
+    dims = [4, 4, 4, 4]
+    for g in (1, 2, 3):
+        U = oracle.random_gauge(g, 2, dims, 3)
+        h = oracle.random_transform(g, 2, dims, 5)
+        Ug = oracle.gauge_transform(g, 2, dims, U, h)
+        assert oracle.plaquette(g, 2, dims, Ug) == pytest.approx(oracle.plaquette(g, 2, dims, U), abs=1e-13)
+
+
+def test_landau_overrelaxation_converges(oracle):
+    dims = [4, 4, 4, 4]
+    for g in (1, 2, 3):
+        U = oracle.random_gauge(g, 2, dims, 3)
+        U, _ = oracle.hmc_chain(g, 2, dims, U, {1: 2.0, 2: 2.5, 3: 6.0}[g], oracle.make_deltas("2lf", 0.5, 10),
+                                5, 0, 10)
+        gt = oracle.unit_transform(g, 2, dims)
+        f0 = oracle.landau_functional(g, 2, dims, U, gt)
+        gt, sweeps, theta = oracle.landau_or(g, 2, dims, U, gt, 1.7, 1e-12, 5000, 10)
+        assert theta < 1e-12
+        th2, fn = oracle.landau_theta(g, 2, dims, U, gt)
+        assert th2 == pytest.approx(oracle.landau_condition(g, 2, dims, U, gt), rel=1e-6, abs=1e-16)
+        assert fn > f0 and fn == pytest.approx(oracle.landau_functional(g, 2, dims, U, gt), rel=1e-12)
