@@ -46,7 +46,13 @@ def parse():
     ap.add_argument("--therm", type=int, default=WORKLOAD["therm"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--lattice", type=int, default=32,
+                    help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
+    a = ap.parse_args()
+    if a.lattice != 32:
+        WORKLOAD["dims"] = [a.lattice] * 4
+        WORKLOAD["name"] = WORKLOAD["name"].replace("32^4", f"{a.lattice}^4")
+    return a
 
 
 def sizes(dims, prec_bytes=4):
@@ -190,7 +196,7 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD["name"], "lattice": dims, "beta": WORKLOAD["beta"],
                        "integrator": f"{WORKLOAD['scheme']} eps={WORKLOAD['eps']} n={WORKLOAD['substeps']}",
-                       "parallelism": "cpu threads"},
+                       "precision": "FP32 (the reference's precision=1 path)", "parallelism": "cpu threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -17,6 +17,32 @@ struct mesh_ctx_s
 {
 	Context c;
 };
+
+namespace {
+void teardown_ctx(Context &c)
+{
+	cudaSetDevice(c.device);
+	if (c.stream)
+		cudaStreamSynchronize(c.stream);
+	cudaFree(c.d_partials);
+	cudaFree(c.d_results);
+	cudaFree(c.d_counters);
+	if (c.d_stage)
+		cudaFree(c.d_stage);
+	if (c.own_stream && c.stream)
+		cudaStreamDestroy(c.stream);
+}
+
+// drops one owner of the context; frees it with the last one
+void release_ctx(Context *c)
+{
+	if (c && --c->refs == 0)
+	{
+		teardown_ctx(*c);
+		delete reinterpret_cast<mesh_ctx_s *>(c);
+	}
+}
+} // namespace
 struct mesh_field_s
 {
 	Field f;
@@ -94,16 +120,22 @@ void create_field(Context &c, int kind, int group, int prec, int nd, int32_t con
 	f.bytes = size_t(nstack) * size_t(V) * size_t(f.nr) * f.real_bytes;
 	DeviceGuard dg(c.device);
 	MESH_CUDA(cudaMalloc(&f.d, f.bytes));
+	++c.refs;
 }
 
 void destroy_field(Field &f)
 {
 	if (f.d)
 	{
-		DeviceGuard dg(f.ctx->device);
-		cudaFree(f.d);
+		{
+			DeviceGuard dg(f.ctx->device);
+			cudaStreamSynchronize(f.ctx->stream);
+			cudaFree(f.d);
+		}
+		release_ctx(f.ctx);
 	}
 	f.d = nullptr;
+	f.ctx = nullptr;
 }
 
 void same_shape(Field const &a, Field const &b)
@@ -356,22 +388,10 @@ int mesh_ctx_create(int device, void *stream, mesh_ctx *out)
 
 int mesh_ctx_destroy(mesh_ctx h)
 {
-	if (!h)
-		return MESH_OK;
-	{
-		Context &c = h->c;
-		cudaSetDevice(c.device);
-		if (c.stream)
-			cudaStreamSynchronize(c.stream);
-		cudaFree(c.d_partials);
-		cudaFree(c.d_results);
-		cudaFree(c.d_counters);
-		if (c.d_stage)
-			cudaFree(c.d_stage);
-		if (c.own_stream && c.stream)
-			cudaStreamDestroy(c.stream);
-	}
-	delete h;
+	// releases the caller's reference; fields and chains still alive keep
+	// the context until they are destroyed
+	if (h)
+		release_ctx(&h->c);
 	return MESH_OK;
 }
 
@@ -725,15 +745,16 @@ int mesh_hmc_destroy(mesh_hmc h)
 		cudaSetDevice(h->ctx->device);
 		cudaStreamSynchronize(h->ctx->stream);
 		h->drop_graph();
-		destroy_field(h->U.f);
-		destroy_field(h->Unew.f);
-		destroy_field(h->P.f);
 		cudaFree(h->d_dev);
 		cudaFree(h->d_hist);
 		cudaFree(h->d_flag);
 		cudaFree(h->d_part);
 		cudaFree(h->d_res);
 		cudaFree(h->d_cnt);
+		// the fields hold the chain's references to the context
+		destroy_field(h->U.f);
+		destroy_field(h->Unew.f);
+		destroy_field(h->P.f);
 	}
 	delete h;
 	return MESH_OK;

@@ -44,6 +44,9 @@ constexpr int kMaxRedBlocks = 4096;
 
 struct Context
 {
+	// owners: the caller's handle plus every field and chain created on it;
+	// the context is torn down when the last one is released
+	int refs = 1;
 	int device = 0;
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
