@@ -309,7 +309,8 @@ def run_ours(args):
                        "trajectory_algorithmic_GB": algorithmic_bytes_per_traj(dims, n) / 1e9,
                        "trajectory_effective_GBps": algorithmic_bytes_per_traj(dims, n) / (ms / args.steps / 1e3)
                        / 1e9},
-           "clocks": clk, "gpu_launches": launches_per_traj * args.steps}
+           "clocks": clk, "gpu_launches": launches_per_traj * args.steps,
+           "autotune": mg.tune_report().strip().splitlines()}
 
     # end to end through the C ABI with host buffers: the gauge field in the
     # reference's host layout is imported, one trajectory runs, the field is

@@ -23,7 +23,7 @@
  *    device they are packed (1/3/8 reals).
  *  - Device storage is even/odd checkerboard, structure-of-arrays
  *    (mesh_field_device_ptr documents nothing more: treat it as opaque).
- *  - All extents must be even, 2 <= nd <= 4, and the volume < 2^31.
+ *  - All extents must be even and below 256, 2 <= nd <= 4, volume < 2^31.
  *  - Calls are issued on the context's stream. Functions returning a host
  *    scalar synchronise that stream (as the reference's reductions do,
  *    src/lattice/device.h:259-260); the others are asynchronous.
@@ -67,6 +67,13 @@ typedef struct mesh_hmc_s *mesh_hmc;
 const char *mesh_last_error(void);
 /* ABI version: major*10000 + minor*100 + patch */
 int mesh_version(void);
+
+/* Autotuner report: one line per tuned kernel/lattice key with the chosen
+ * launch variant and the measured candidates. Writes at most cap bytes
+ * (NUL-terminated) and returns the size needed. Tuning runs once per key and
+ * process, on the first call outside a stream capture; MESH_AUTOTUNE=0 in the
+ * environment disables it (default variants). */
+size_t mesh_tune_report(char *buf, size_t cap);
 
 /* ---- context: device + stream + reduction scratch ------------------------
  * Replaces the reference's implicit "current device, default stream"

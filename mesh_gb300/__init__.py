@@ -58,6 +58,7 @@ class HmcRecord(C.Structure):
 SIGNATURES = {
     "mesh_last_error": (C.c_char_p, []),
     "mesh_version": (_I, []),
+    "mesh_tune_report": (_SZ, [C.c_char_p, _SZ]),
     "mesh_ctx_create": (_I, [_I, _P, _PP]),
     "mesh_ctx_destroy": (_I, [_P]),
     "mesh_ctx_synchronize": (_I, [_P]),
@@ -113,6 +114,15 @@ class MeshError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"{STATUS.get(code, code)}: {msg}")
         self.code = code
+
+
+def tune_report() -> str:
+    """Launch variants chosen by the autotuner so far (one line per key)."""
+    L = load()
+    n = L.mesh_tune_report(None, 0)
+    buf = C.create_string_buffer(n)
+    L.mesh_tune_report(buf, n)
+    return buf.value.decode()
 
 
 def lib_path() -> str:

@@ -102,6 +102,7 @@ void create_field(Context &c, int kind, int group, int prec, int nd, int32_t con
 	for (int i = 0; i < nd; ++i)
 	{
 		require(dims[i] >= 2 && dims[i] % 2 == 0, "every extent must be even and >= 2 (checkerboard layout)");
+		require(dims[i] < 256, "every extent must be below 256");
 		V *= dims[i];
 		require(V < (int64_t(1) << 31), "volume must be below 2^31");
 	}
@@ -856,6 +857,8 @@ int mesh_hmc_run(mesh_hmc h, double beta, double const *deltas, int n, int count
 			ops_for(h->U.f).plaquette(h->U.f, h->rs(mesh_hmc_s::S_CUR));
 			h->S_valid = true;
 		}
+		// choose launch variants before capturing (tuning times kernels)
+		ops_for(h->U.f).tune(h->P.f, h->Unew.f);
 		std::vector<double> dv(deltas, deltas + n);
 		if (!h->graph || h->graph_beta != beta || h->graph_deltas != dv || h->graph_hist != h->d_hist)
 		{

@@ -6,6 +6,7 @@
 #include "layout.cuh"
 #include "reduce.cuh"
 
+#include <string>
 #include <vector>
 
 namespace meshgb {
@@ -103,7 +104,15 @@ struct OpsTable
 	void (*exp_apply)(Field &dst, Field const &F, double eps, Field const &g);
 	void (*axpy_alg)(Field &y, double a, Field const &x);
 	void (*gauge_transform)(Field &U, Field const &g);
+	// pick launch variants for U's lattice ahead of a stream capture
+	void (*tune)(Field &P, Field const &U);
 };
+
+// autotuning registry (tune.cu): variant index per kernel/lattice key
+int tuned_variant(std::string const &key);
+void set_tuned_variant(std::string const &key, int variant, std::string const &report);
+bool autotune_enabled();
+std::string tune_report();
 
 OpsTable const *ops_u1(int prec, int nd);
 OpsTable const *ops_su2(int prec, int nd);

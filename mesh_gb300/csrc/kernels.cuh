@@ -7,6 +7,7 @@
 #include "group.cuh"
 #include "rng.cuh"
 
+#include <string>
 #include <type_traits>
 
 namespace meshgb {
@@ -197,10 +198,11 @@ __global__ void __launch_bounds__(kBlock)
 	MESH_GRID_LOOP(s, g.V)
 	{
 		Site<ND> st = site_from_eo<ND>(g, s);
-		int L = g.L[dir];
-		int xn = ((st.x[dir] + offset) % L + L) % L;
-		int64_t lex = st.lex + int64_t(xn - st.x[dir]) * g.stride[dir];
-		int par = (st.par + (xn - st.x[dir])) & 1;
+		int L = g.Ld(dir);
+		int x0 = st.x(dir);
+		int xn = ((x0 + offset) % L + L) % L;
+		int64_t lex = st.lex + int64_t(xn - x0) * g.Sd(dir);
+		int par = (st.par + (xn - x0)) & 1;
 		int64_t sn = int64_t(par) * g.Vh + (lex >> 1);
 		T v[Gp::NR];
 		Soa<T, Gp::NR>::load(src, g.V, sn, v);
@@ -294,33 +296,34 @@ __global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restric
 	grid_sum<kBlock>(acc, out);
 }
 
-// staple sum for link (x, mu) in the reference's association order
-// (utils.h:129-136): upper U_nu(x+mu) (U_nu(x) U_mu(x+nu))^+, lower
-// (U_mu(y) U_nu(y+mu))^+ U_nu(y) at y = x - nu. MU is a template argument so
-// that every coordinate access is static (no local-memory indexing).
-template <int GRP, class T, int ND, int MU>
-__device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<ND> const &st, int64_t s,
+// staple sum for link (x, mu) in the reference's association and summation
+// order (utils.h:119-137): for nu = 0..Nd-1, nu != mu, the upper staple
+// U_nu(x+mu) (U_nu(x) U_mu(x+nu))^+ then the lower staple
+// (U_mu(y) U_nu(y+mu))^+ U_nu(y) at y = x - nu. Runtime mu and a rolled nu
+// loop keep one copy of the SU(3) body in the instruction cache.
+template <int GRP, class T, int ND>
+__device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<ND> const &st, int64_t s, int mu,
                                                             LinkLoad<GRP, T, ND> const &ld)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	E S = Gp::zero();
-	int64_t xpm = eo_shift1<ND>(g, st, MU, +1);
-#pragma unroll
+	int64_t xpm = eo_shift1<ND>(g, st, mu, +1);
+#pragma unroll 1
 	for (int nu = 0; nu < ND; ++nu)
 	{
-		if (nu == MU)
+		if (nu == mu)
 			continue;
 		{
 			E b = ld(nu, xpm);
-			E c = ld(MU, eo_shift1<ND>(g, st, nu, +1));
+			E c = ld(mu, eo_shift1<ND>(g, st, nu, +1));
 			E d = ld(nu, s);
 			Gp::add_to(S, Gp::mul_nd(b, Gp::mul(d, c)));
 		}
 		{
 			int64_t y = eo_shift1<ND>(g, st, nu, -1);
-			E e = ld(MU, y);
-			E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, MU, +1));
+			E e = ld(mu, y);
+			E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
 			E h = ld(nu, y);
 			Gp::add_to(S, Gp::mul_dn(Gp::mul(e, f), h));
 		}
@@ -328,62 +331,93 @@ __device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<
 	return S;
 }
 
-// calls f(std::integral_constant<int, mu>) for a runtime direction mu < ND
-template <int ND, class Fn> __device__ __forceinline__ void with_mu(int mu, Fn &&f)
-{
-	switch (mu)
-	{
-	case 0:
-		f(std::integral_constant<int, 0>{});
-		break;
-	case 1:
-		f(std::integral_constant<int, 1>{});
-		break;
-	case 2:
-		if constexpr (ND > 2)
-			f(std::integral_constant<int, 2>{});
-		break;
-	default:
-		if constexpr (ND > 3)
-			f(std::integral_constant<int, 3>{});
-		break;
-	}
-}
-
-// P_mu(x) -= coef * proj(U_mu(x) S_mu(x)) with coef = beta/(2 Nc) * delta,
-// one thread per (site, mu); optionally sums norm2 of the updated momenta
-template <int GRP, class T, int ND, bool KIN>
-__global__ void __launch_bounds__(kBlock)
-    k_momentum_step(Geom g, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin)
+// one link's momentum update: P_mu(x) -= coef proj(U_mu(x) S_mu(x)); returns
+// the kinetic norm of the updated momentum
+template <int GRP, class T, int ND>
+__device__ __forceinline__ double force_item(Geom const &g, Site<ND> const &st, int64_t s, int mu,
+                                             LinkLoad<GRP, T, ND> const &ld, T *__restrict__ P, T coef)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
+	E S = staple<GRP, T, ND>(g, st, s, mu, ld);
+	E W = Gp::mul(ld(mu, s), S);
+	T f[Gp::NA], p[Gp::NA];
+	Gp::proj(W, f);
+	auto Pv = comp<T, Gp::NA>(P, g.V, mu);
+	Pv.load(s, p);
+#pragma unroll
+	for (int k = 0; k < Gp::NA; ++k)
+		p[k] -= coef * f[k];
+	Pv.store(s, p);
+	return double(Gp::kin(p));
+}
+
+// Momentum step, one thread per (site, mu) in even/odd order.
+template <int GRP, class T, int ND, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_momentum_step(Geom g, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin)
+{
 	LinkLoad<GRP, T, ND> ld{U, g.V};
 	double acc = 0.0;
 	int64_t n = int64_t(ND) * g.V;
-	MESH_GRID_LOOP(i, n)
+	for (int64_t i = int64_t(blockIdx.x) * NT + threadIdx.x; i < n; i += int64_t(gridDim.x) * NT)
 	{
 		int mu = int(i / g.V);
 		int64_t s = i - int64_t(mu) * g.V;
 		Site<ND> st = site_from_eo<ND>(g, s);
-		with_mu<ND>(mu, [&](auto MUc) {
-			constexpr int MU = decltype(MUc)::value;
-			E S = staple<GRP, T, ND, MU>(g, st, s, ld);
-			E W = Gp::mul(ld(MU, s), S);
-			T f[Gp::NA], p[Gp::NA];
-			Gp::proj(W, f);
-			auto Pv = comp<T, Gp::NA>(P, g.V, MU);
-			Pv.load(s, p);
-#pragma unroll
-			for (int k = 0; k < Gp::NA; ++k)
-				p[k] -= coef * f[k];
-			Pv.store(s, p);
-			if constexpr (KIN)
-				acc += double(Gp::kin(p));
-		});
+		acc += force_item<GRP, T, ND>(g, st, s, mu, ld, P, coef);
 	}
-	if constexpr (KIN)
-		grid_sum<kBlock>(acc, kin);
+	if (kin.result)
+		grid_sum<NT>(acc, kin);
+}
+
+// 4D tile of sites handled by one block: extents 2^lt[i], tiles per
+// dimension nt[i]; a block walks its tile's sites lexicographically and all
+// directions of each site, so neighbour links are reused from L1.
+struct TileSpec
+{
+	int lt[4];
+	int nt[4];
+	int sites;  // sites per tile
+	int ntiles; // tiles in the lattice
+};
+
+template <int GRP, class T, int ND, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_momentum_step_tiled(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin)
+{
+	LinkLoad<GRP, T, ND> ld{U, g.V};
+	double acc = 0.0;
+	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
+	{
+		int origin[ND];
+		int r = tile;
+#pragma unroll
+		for (int i = ND - 1; i >= 0; --i)
+		{
+			int q = r / ts.nt[i];
+			origin[i] = (r - q * ts.nt[i]) << ts.lt[i];
+			r = q;
+		}
+		for (int t = threadIdx.x; t < ts.sites; t += NT)
+		{
+			int x[ND];
+			int rr = t;
+#pragma unroll
+			for (int i = ND - 1; i >= 0; --i)
+			{
+				x[i] = origin[i] + (rr & ((1 << ts.lt[i]) - 1));
+				rr >>= ts.lt[i];
+			}
+			Site<ND> st = site_from_coords<ND>(g, x);
+			int64_t s = eo_of<ND>(g, st);
+#pragma unroll 1
+			for (int mu = 0; mu < ND; ++mu)
+				acc += force_item<GRP, T, ND>(g, st, s, mu, ld, P, coef);
+		}
+	}
+	if (kin.result)
+		grid_sum<NT>(acc, kin);
 }
 
 template <int GRP, class T, int ND>
@@ -394,10 +428,8 @@ __global__ void __launch_bounds__(kBlock) k_staple_sum(Geom g, int mu, T const *
 	MESH_GRID_LOOP(s, g.V)
 	{
 		Site<ND> st = site_from_eo<ND>(g, s);
-		with_mu<ND>(mu, [&](auto MUc) {
-			auto e = staple<GRP, T, ND, decltype(MUc)::value>(g, st, s, ld);
-			Soa<T, Gp::NR>::store(S, g.V, s, e.v);
-		});
+		auto e = staple<GRP, T, ND>(g, st, s, mu, ld);
+		Soa<T, Gp::NR>::store(S, g.V, s, e.v);
 	}
 }
 
@@ -411,17 +443,14 @@ __global__ void __launch_bounds__(kBlock)
 	MESH_GRID_LOOP(s, g.V)
 	{
 		Site<ND> st = site_from_eo<ND>(g, s);
-		with_mu<ND>(mu, [&](auto MUc) {
-			constexpr int MU = decltype(MUc)::value;
-			E S = staple<GRP, T, ND, MU>(g, st, s, ld);
-			E W = Gp::mul(ld(MU, s), S);
-			T f[Gp::NA];
-			Gp::proj(W, f);
+		E S = staple<GRP, T, ND>(g, st, s, mu, ld);
+		E W = Gp::mul(ld(mu, s), S);
+		T f[Gp::NA];
+		Gp::proj(W, f);
 #pragma unroll
-			for (int k = 0; k < Gp::NA; ++k)
-				f[k] *= scale;
-			Soa<T, Gp::NA>::store(F, g.V, s, f);
-		});
+		for (int k = 0; k < Gp::NA; ++k)
+			f[k] *= scale;
+		Soa<T, Gp::NA>::store(F, g.V, s, f);
 	}
 }
 
@@ -937,17 +966,137 @@ template <int GRP, class T, int ND> struct Ops
 			    static_cast<T const *>(P.d), T(t));
 		MESH_LAUNCH_CHECK();
 	}
-	static void momentum_step(Field &P, Field const &U, double coef, RedSlot *kin)
+	// ---- momentum step: launch variants and their autotuning ----------------
+	struct ForceVariant
+	{
+		int tiled;
+		int lt[4]; // log2 tile extents
+		int threads, minb;
+		char const *name;
+	};
+	static int n_force_variants() { return ND == 4 ? 8 : 2; }
+	static ForceVariant force_variant(int v)
+	{
+		static const ForceVariant t[8] = {
+		    {0, {0, 0, 0, 0}, 256, 1, "eo-order/256thr/1blk"},   {0, {0, 0, 0, 0}, 256, 2, "eo-order/256thr/2blk"},
+		    {1, {2, 2, 2, 2}, 256, 1, "tile4x4x4x4/256thr/1blk"}, {1, {2, 2, 2, 2}, 256, 2, "tile4x4x4x4/256thr/2blk"},
+		    {1, {1, 2, 2, 2}, 128, 3, "tile2x4x4x4/128thr/3blk"}, {1, {1, 2, 2, 2}, 128, 4, "tile2x4x4x4/128thr/4blk"},
+		    {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk"}, {1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk"}};
+		return t[v];
+	}
+	static bool force_variant_valid(Geom const &g, int v)
+	{
+		ForceVariant fv = force_variant(v);
+		if (!fv.tiled)
+			return true;
+		if (ND != 4)
+			return false;
+		for (int i = 0; i < 4; ++i)
+			if (g.L[i] % (1 << fv.lt[i]) != 0)
+				return false;
+		return true;
+	}
+	static void launch_force(int v, Field &P, Field const &U, T coef, RedSlot kin)
 	{
 		auto &c = *U.ctx;
-		int64_t n = int64_t(ND) * U.geom.V;
-		if (kin)
-			k_momentum_step<GRP, T, ND, true><<<red_blocks(c, n), kBlock, 0, c.stream>>>(
-			    U.geom, static_cast<T const *>(U.d), static_cast<T *>(P.d), T(coef), *kin);
-		else
-			k_momentum_step<GRP, T, ND, false><<<blocks(c, n), kBlock, 0, c.stream>>>(
-			    U.geom, static_cast<T const *>(U.d), static_cast<T *>(P.d), T(coef), RedSlot{});
+		Geom const &g = U.geom;
+		ForceVariant fv = force_variant(v);
+		T const *u = static_cast<T const *>(U.d);
+		T *p = static_cast<T *>(P.d);
+		if (!fv.tiled)
+		{
+			int64_t n = int64_t(ND) * g.V;
+			unsigned b = grid_for(c, n, fv.threads, fv.minb * 2);
+			if (b > unsigned(kMaxRedBlocks))
+				b = kMaxRedBlocks;
+			if (fv.minb == 1)
+				k_momentum_step<GRP, T, ND, 256, 1><<<b, 256, 0, c.stream>>>(g, u, p, coef, kin);
+			else
+				k_momentum_step<GRP, T, ND, 256, 2><<<b, 256, 0, c.stream>>>(g, u, p, coef, kin);
+		}
+		else if constexpr (ND == 4)
+		{
+			TileSpec ts{};
+			ts.sites = 1;
+			ts.ntiles = 1;
+			for (int i = 0; i < 4; ++i)
+			{
+				ts.lt[i] = fv.lt[i];
+				ts.nt[i] = g.L[i] >> fv.lt[i];
+				ts.sites <<= fv.lt[i];
+				ts.ntiles *= ts.nt[i];
+			}
+			int64_t cap = int64_t(c.num_sms) * fv.minb;
+			unsigned b = unsigned(ts.ntiles < cap ? ts.ntiles : cap);
+			if (fv.threads == 256 && fv.minb == 1)
+				k_momentum_step_tiled<GRP, T, 4, 256, 1><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+			else if (fv.threads == 256 && fv.minb == 2)
+				k_momentum_step_tiled<GRP, T, 4, 256, 2><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+			else if (fv.threads == 128 && fv.minb == 3)
+				k_momentum_step_tiled<GRP, T, 4, 128, 3><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+			else
+				k_momentum_step_tiled<GRP, T, 4, 128, 4><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+		}
 		MESH_LAUNCH_CHECK();
+	}
+	static std::string force_key(Field const &U)
+	{
+		std::string k = "momentum_step/group" + std::to_string(GRP) + "/" + (sizeof(T) == 4 ? "f32" : "f64") + "/";
+		for (int i = 0; i < ND; ++i)
+			k += (i ? "x" : "") + std::to_string(U.dims[i]);
+		return k;
+	}
+	// fastest valid variant for this lattice, timed once with coef = 0 (the
+	// momenta are rewritten unchanged); not while the stream is capturing
+	static int choose_force(Field &P, Field const &U)
+	{
+		std::string key = force_key(U);
+		int v = tuned_variant(key);
+		if (v >= 0)
+			return v;
+		int dflt = force_variant_valid(U.geom, 3) ? 3 : 0;
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		cudaStreamIsCapturing(U.ctx->stream, &cs);
+		if (cs != cudaStreamCaptureStatusNone || !autotune_enabled())
+			return dflt;
+		auto &c = *U.ctx;
+		cudaEvent_t e0, e1;
+		MESH_CUDA(cudaEventCreate(&e0));
+		MESH_CUDA(cudaEventCreate(&e1));
+		float best = 1e30f;
+		int bestv = dflt;
+		std::string report;
+		for (int cand = 0; cand < n_force_variants(); ++cand)
+		{
+			if (!force_variant_valid(U.geom, cand))
+				continue;
+			launch_force(cand, P, U, T(0), RedSlot{});
+			MESH_CUDA(cudaEventRecord(e0, c.stream));
+			for (int r = 0; r < 3; ++r)
+				launch_force(cand, P, U, T(0), RedSlot{});
+			MESH_CUDA(cudaEventRecord(e1, c.stream));
+			MESH_CUDA(cudaEventSynchronize(e1));
+			float ms = 0;
+			MESH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+			ms /= 3;
+			report += std::string(report.empty() ? "" : ", ") + force_variant(cand).name + "=" +
+			          std::to_string(ms * 1000.0f) + "us";
+			if (ms < best)
+			{
+				best = ms;
+				bestv = cand;
+			}
+		}
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		set_tuned_variant(key, bestv, std::string("chosen ") + force_variant(bestv).name + " [" + report + "]");
+		return bestv;
+	}
+	static void tune(Field &P, Field const &U) { choose_force(P, U); }
+	static void momentum_step(Field &P, Field const &U, double coef, RedSlot *kin)
+	{
+		int v = choose_force(P, U);
+		launch_force(v, P, U, T(coef), kin ? *kin : RedSlot{});
 	}
 	static void landau_functional(Field const &U, Field const &g, RedSlot out)
 	{
@@ -1015,7 +1164,7 @@ template <int GRP, class T, int ND> struct Ops
 		                           cshift,       site_op,       sum_real_trace, plaquette,      staple_sum,
 		                           wilson_deriv, reunitize,     evolve,         momentum_step,  landau_functional,
 		                           landau_theta, landau_deriv,  landau_or_half, reunit_exact,   alg_dot,
-		                           exp_apply,    axpy_alg,      gauge_transform};
+		                           exp_apply,    axpy_alg,      gauge_transform, tune};
 		return &t;
 	}
 };

@@ -31,6 +31,18 @@ struct Geom
 	int L[4];
 	int64_t V, Vh;
 	int64_t stride[4]; // lexicographic stride of dimension i
+
+	// extent / stride of a runtime direction through selects on constant
+	// offsets (indexing the kernel-parameter arrays with a runtime index
+	// would copy the struct to local memory)
+	__host__ __device__ __forceinline__ int Ld(int d) const
+	{
+		return d == 0 ? L[0] : d == 1 ? L[1] : d == 2 ? L[2] : L[3];
+	}
+	__host__ __device__ __forceinline__ int32_t Sd(int d) const
+	{
+		return int32_t(d == 0 ? stride[0] : d == 1 ? stride[1] : d == 2 ? stride[2] : stride[3]);
+	}
 };
 
 inline Geom make_geom(int nd, int32_t const *dims)
@@ -51,13 +63,15 @@ inline Geom make_geom(int nd, int32_t const *dims)
 	return g;
 }
 
-// Coordinates, lexicographic index and parity of the site with even/odd
-// index s.
+// Coordinates, lexicographic index and parity of a site. The coordinates are
+// packed 8 bits per dimension into one register (extents < 256), so that a
+// runtime direction selects one with a shift: no local-memory arrays.
 template <int ND> struct Site
 {
-	int x[ND];
-	int64_t lex;
-	int par;
+	uint32_t px;  // coordinate i in bits [8i, 8i+8)
+	int32_t lex;  // lexicographic index (V < 2^31)
+	int par;      // parity of the coordinate sum
+	__device__ __forceinline__ int x(int i) const { return int((px >> (8 * i)) & 0xffu); }
 };
 
 template <int ND> __device__ __forceinline__ Site<ND> site_from_eo(Geom const &g, int64_t s)
@@ -67,61 +81,81 @@ template <int ND> __device__ __forceinline__ Site<ND> site_from_eo(Geom const &g
 	// V < 2^31 is enforced at field creation: 32-bit division suffices
 	uint32_t r = uint32_t(s - p * g.Vh) * 2u;
 	int sum = 0;
+	uint32_t px = 0;
 #pragma unroll
 	for (int i = ND - 1; i >= 0; --i)
 	{
 		uint32_t L = uint32_t(g.L[i]);
 		uint32_t q = r / L;
-		st.x[i] = int(r - q * L);
+		uint32_t xi = r - q * L;
+		px |= xi << (8 * i);
 		r = q;
-		sum += st.x[i];
+		sum += int(xi);
 	}
-	int64_t lex = (s - p * g.Vh) * 2;
+	int32_t lex = int32_t(s - p * g.Vh) * 2;
 	if ((sum & 1) != p)
 	{
-		st.x[ND - 1] += 1;
+		px += 1u << (8 * (ND - 1));
 		lex += 1;
 	}
+	st.px = px;
 	st.lex = lex;
 	st.par = p;
 	return st;
 }
 
-// even/odd index of the neighbour site at x + d (d a small signed offset
-// vector given as (dir, sign) pairs). Single-step neighbour:
+// site with the given coordinates (each in range)
+template <int ND> __device__ __forceinline__ Site<ND> site_from_coords(Geom const &g, int const *x)
+{
+	Site<ND> st;
+	uint32_t px = 0;
+	int32_t lex = 0;
+	int sum = 0;
+#pragma unroll
+	for (int i = 0; i < ND; ++i)
+	{
+		px |= uint32_t(x[i]) << (8 * i);
+		lex = lex * g.L[i] + x[i];
+		sum += x[i];
+	}
+	st.px = px;
+	st.lex = lex;
+	st.par = sum & 1;
+	return st;
+}
+
+template <int ND> __device__ __forceinline__ int64_t eo_of(Geom const &g, Site<ND> const &st)
+{
+	return int64_t(st.par) * g.Vh + (st.lex >> 1);
+}
+
+// lexicographic index after a step of `sign` (+-1) in direction dir
+__device__ __forceinline__ int32_t lex_step(Geom const &g, uint32_t px, int32_t lex, int dir, int sign)
+{
+	int xd = int((px >> (8 * dir)) & 0xffu) + sign;
+	int L = g.Ld(dir);
+	int32_t st = g.Sd(dir);
+	if (xd == L)
+		return lex - (L - 1) * st;
+	if (xd < 0)
+		return lex + (L - 1) * st;
+	return lex + sign * st;
+}
+
+// even/odd index of the neighbour x + sign e_dir (opposite parity)
 template <int ND>
 __device__ __forceinline__ int64_t eo_shift1(Geom const &g, Site<ND> const &st, int dir, int sign)
 {
-	int xd = st.x[dir] + sign;
-	int64_t lex = st.lex;
-	if (xd == g.L[dir])
-		lex -= int64_t(g.L[dir] - 1) * g.stride[dir];
-	else if (xd < 0)
-		lex += int64_t(g.L[dir] - 1) * g.stride[dir];
-	else
-		lex += sign * g.stride[dir];
+	int32_t lex = lex_step(g, st.px, st.lex, dir, sign);
 	return int64_t(st.par ^ 1) * g.Vh + (lex >> 1);
 }
 
-// neighbour at x + s1*e_d1 + s2*e_d2 (d1 != d2); same parity as x
+// neighbour at x + s1 e_d1 + s2 e_d2 (d1 != d2); same parity as x
 template <int ND>
 __device__ __forceinline__ int64_t eo_shift2(Geom const &g, Site<ND> const &st, int d1, int s1, int d2, int s2)
 {
-	int64_t lex = st.lex;
-	int a = st.x[d1] + s1;
-	if (a == g.L[d1])
-		lex -= int64_t(g.L[d1] - 1) * g.stride[d1];
-	else if (a < 0)
-		lex += int64_t(g.L[d1] - 1) * g.stride[d1];
-	else
-		lex += s1 * g.stride[d1];
-	int b = st.x[d2] + s2;
-	if (b == g.L[d2])
-		lex -= int64_t(g.L[d2] - 1) * g.stride[d2];
-	else if (b < 0)
-		lex += int64_t(g.L[d2] - 1) * g.stride[d2];
-	else
-		lex += s2 * g.stride[d2];
+	int32_t lex = lex_step(g, st.px, st.lex, d1, s1);
+	lex = lex_step(g, st.px, lex, d2, s2);
 	return int64_t(st.par) * g.Vh + (lex >> 1);
 }
 

@@ -1,0 +1,60 @@
+// Autotuner registry: the launch variant chosen per (kernel, group,
+// precision, lattice) key, measured once per process with CUDA events on the
+// context's stream (kernels.cuh, Ops::choose_force). MESH_AUTOTUNE=0 in the
+// environment disables timing and uses the default variants.
+#include "field.cuh"
+
+#include <cstdlib>
+#include <map>
+#include <mutex>
+
+namespace meshgb {
+namespace {
+std::mutex g_mu;
+std::map<std::string, std::pair<int, std::string>> &registry()
+{
+	static std::map<std::string, std::pair<int, std::string>> m;
+	return m;
+}
+} // namespace
+
+int tuned_variant(std::string const &key)
+{
+	std::lock_guard<std::mutex> lk(g_mu);
+	auto it = registry().find(key);
+	return it == registry().end() ? -1 : it->second.first;
+}
+
+void set_tuned_variant(std::string const &key, int variant, std::string const &report)
+{
+	std::lock_guard<std::mutex> lk(g_mu);
+	registry()[key] = {variant, report};
+}
+
+bool autotune_enabled()
+{
+	char const *e = std::getenv("MESH_AUTOTUNE");
+	return !(e && e[0] == '0');
+}
+
+std::string tune_report()
+{
+	std::lock_guard<std::mutex> lk(g_mu);
+	std::string r;
+	for (auto const &[k, v] : registry())
+		r += k + ": " + v.second + "\n";
+	return r;
+}
+} // namespace meshgb
+
+extern "C" size_t mesh_tune_report(char *buf, size_t cap)
+{
+	std::string r = meshgb::tune_report();
+	if (buf && cap)
+	{
+		size_t n = r.size() < cap - 1 ? r.size() : cap - 1;
+		r.copy(buf, n);
+		buf[n] = '\0';
+	}
+	return r.size() + 1;
+}

@@ -45,9 +45,10 @@ def momenta(ctx, g, p, dims, arr):
 
 
 def thermal(oracle, g, dims, seed=3, ntraj=3):
-    """A (partly) thermalised FP64 configuration from the oracle's chain."""
-    U = oracle.random_gauge(g, 2, dims, seed)
-    U, _ = oracle.hmc_chain(g, 2, dims, U, BETA[g] + 1.0, oracle.make_deltas("2lf", 0.5, 8), seed, 0, ntraj)
+    """A partly thermalised FP64 configuration: a few trajectories of the
+    oracle's chain from a cold start (plaquette well away from 0 and 1)."""
+    U = oracle.unit_gauge(g, 2, dims)
+    U, _ = oracle.hmc_chain(g, 2, dims, U, BETA[g], oracle.make_deltas("2lf", 0.5, 8), seed, 0, ntraj)
     return U
 
 
@@ -137,7 +138,11 @@ def test_plaquette_action_vs_oracle(ctx, oracle, g, p, dims):
     U64 = thermal(oracle, g, dims)
     U = gauge(ctx, g, p, dims, U64.astype(mg.real_dtype(p)))
     ref = oracle.plaquette(g, 2, dims, U64)
-    assert mg.plaquette(U) == pytest.approx(ref, rel=1e-13 if p == 2 else 1e-6)
+    assert mg.plaquette(U) == pytest.approx(ref, rel=1e-13, abs=1e-15) if p == 2 else \
+        mg.plaquette(U) == pytest.approx(ref, abs=1e-6)
+    U_hot = gauge(ctx, g, p, dims, oracle.random_gauge(g, p, dims, 8))
+    assert mg.plaquette(U_hot) == pytest.approx(oracle.plaquette(g, 2, dims, oracle.random_gauge(g, 2, dims, 8)),
+                                                abs=1e-14 if p == 2 else 1e-6)
     S = oracle.wilson_action(g, 2, dims, U64, BETA[g])
     assert mg.wilson_action(U, BETA[g]) == pytest.approx(S, rel=1e-12 if p == 2 else 1e-5)
     cold = mg.GaugeField(ctx, g, p, mg.Grid(dims)).set_unit()
