@@ -74,6 +74,10 @@ int mesh_version(void);
  * process, on the first call outside a stream capture; MESH_AUTOTUNE=0 in the
  * environment disables it (default variants). */
 size_t mesh_tune_report(char *buf, size_t cap);
+/* Forces launch variant `variant` of the fused momentum-step kernel for all
+ * later calls where it is valid for the lattice (-1 restores autotuning).
+ * For testing every variant against the oracle. */
+int mesh_tune_force_variant(int variant);
 
 /* ---- context: device + stream + reduction scratch ------------------------
  * Replaces the reference's implicit "current device, default stream"

@@ -59,6 +59,7 @@ SIGNATURES = {
     "mesh_last_error": (C.c_char_p, []),
     "mesh_version": (_I, []),
     "mesh_tune_report": (_SZ, [C.c_char_p, _SZ]),
+    "mesh_tune_force_variant": (_I, [_I]),
     "mesh_ctx_create": (_I, [_I, _P, _PP]),
     "mesh_ctx_destroy": (_I, [_P]),
     "mesh_ctx_synchronize": (_I, [_P]),
@@ -123,6 +124,11 @@ def tune_report() -> str:
     buf = C.create_string_buffer(n)
     L.mesh_tune_report(buf, n)
     return buf.value.decode()
+
+
+def force_variant(v: int) -> None:
+    """Force launch variant v of the momentum-step kernel (-1: autotune)."""
+    _chk(load().mesh_tune_force_variant(v))
 
 
 def lib_path() -> str:

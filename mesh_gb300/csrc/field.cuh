@@ -112,6 +112,9 @@ struct OpsTable
 int tuned_variant(std::string const &key);
 void set_tuned_variant(std::string const &key, int variant, std::string const &report);
 bool autotune_enabled();
+// forced launch variant of the momentum step (-1: autotune)
+int force_override();
+void set_force_override(int v);
 std::string tune_report();
 
 OpsTable const *ops_u1(int prec, int nd);

@@ -578,4 +578,83 @@ template <class T> struct Group<SU3, T>
 	}
 };
 
+// ---------------------------------------------------------------------------
+// SU(3) float products on the packed FP32x2 FMA (fma.rn.f32x2, sm_100+): a
+// complex multiply-accumulate c += a b is two packed FMAs,
+//   (cr, ci) += (ar, ai) * (br, br);  (cr, ci) += (-ai, ar) * (bi, bi),
+// halving the FMA instruction count of the 3x3 products.
+// ---------------------------------------------------------------------------
+struct Su3F2
+{
+	using E = Group<SU3, float>::E;
+	__device__ __forceinline__ static unsigned long long pk(float a, float b)
+	{
+		unsigned long long r;
+		asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+		return r;
+	}
+	__device__ __forceinline__ static void upk(unsigned long long r, float &a, float &b)
+	{
+		asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+	}
+	__device__ __forceinline__ static unsigned long long fma2(unsigned long long a, unsigned long long b,
+	                                                          unsigned long long c)
+	{
+		unsigned long long d;
+		asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+		return d;
+	}
+	// generic product with operand access functors: c_ij = sum_k A(i,k) B(k,j)
+	// where A(i,k) = (ar, ai) and B(k,j) = (br, bi)
+	template <class FA, class FB> __device__ __forceinline__ static E prod(FA fa, FB fb)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+			unsigned long long an[3], ar[3];
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				float re, im;
+				fa(i, k, re, im);
+				an[k] = pk(re, im);
+				ar[k] = pk(-im, re);
+			}
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				unsigned long long acc = 0ull;
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+				{
+					float re, im;
+					fb(k, j, re, im);
+					acc = fma2(an[k], pk(re, re), acc);
+					acc = fma2(ar[k], pk(im, im), acc);
+				}
+				upk(acc, r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
+			}
+		}
+		return r;
+	}
+	__device__ __forceinline__ static E mul(E const &a, E const &b)
+	{
+		return prod([&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
+		            [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
+	}
+	// a b^dagger: B(k,j) = conj(b_jk)
+	__device__ __forceinline__ static E mul_nd(E const &a, E const &b)
+	{
+		return prod([&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
+		            [&](int k, int j, float &re, float &im) { re = b.v[6 * j + 2 * k]; im = -b.v[6 * j + 2 * k + 1]; });
+	}
+	// a^dagger b: A(i,k) = conj(a_ki)
+	__device__ __forceinline__ static E mul_dn(E const &a, E const &b)
+	{
+		return prod([&](int i, int k, float &re, float &im) { re = a.v[6 * k + 2 * i]; im = -a.v[6 * k + 2 * i + 1]; },
+		            [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
+	}
+};
+
 } // namespace meshgb

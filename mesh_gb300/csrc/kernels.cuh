@@ -259,7 +259,7 @@ template <int GRP, class T, int ND> struct LinkLoad
 	__device__ __forceinline__ E operator()(int mu, int64_t s) const
 	{
 		E e;
-		Soa<T, Gp::NR>::load(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
+		Soa<T, Gp::NR>::template load<CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
 		return e;
 	}
 };
@@ -296,17 +296,35 @@ __global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restric
 	grid_sum<kBlock>(acc, out);
 }
 
+// 3x3 products of the force: packed FP32x2 FMAs for SU(3) float when F2
+template <int GRP, class T, bool F2> struct Prod
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	__device__ __forceinline__ static E mul(E const &a, E const &b) { return Gp::mul(a, b); }
+	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return Gp::mul_nd(a, b); }
+	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return Gp::mul_dn(a, b); }
+};
+template <> struct Prod<SU3, float, true>
+{
+	using E = Group<SU3, float>::E;
+	__device__ __forceinline__ static E mul(E const &a, E const &b) { return Su3F2::mul(a, b); }
+	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return Su3F2::mul_nd(a, b); }
+	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return Su3F2::mul_dn(a, b); }
+};
+
 // staple sum for link (x, mu) in the reference's association and summation
 // order (utils.h:119-137): for nu = 0..Nd-1, nu != mu, the upper staple
 // U_nu(x+mu) (U_nu(x) U_mu(x+nu))^+ then the lower staple
 // (U_mu(y) U_nu(y+mu))^+ U_nu(y) at y = x - nu. Runtime mu and a rolled nu
 // loop keep one copy of the SU(3) body in the instruction cache.
-template <int GRP, class T, int ND>
+template <int GRP, class T, int ND, bool F2 = false>
 __device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<ND> const &st, int64_t s, int mu,
                                                             LinkLoad<GRP, T, ND> const &ld)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
+	using Pr = Prod<GRP, T, F2>;
 	E S = Gp::zero();
 	int64_t xpm = eo_shift1<ND>(g, st, mu, +1);
 #pragma unroll 1
@@ -318,14 +336,14 @@ __device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<
 			E b = ld(nu, xpm);
 			E c = ld(mu, eo_shift1<ND>(g, st, nu, +1));
 			E d = ld(nu, s);
-			Gp::add_to(S, Gp::mul_nd(b, Gp::mul(d, c)));
+			Gp::add_to(S, Pr::mul_nd(b, Pr::mul(d, c)));
 		}
 		{
 			int64_t y = eo_shift1<ND>(g, st, nu, -1);
 			E e = ld(mu, y);
 			E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
 			E h = ld(nu, y);
-			Gp::add_to(S, Gp::mul_dn(Gp::mul(e, f), h));
+			Gp::add_to(S, Pr::mul_dn(Pr::mul(e, f), h));
 		}
 	}
 	return S;
@@ -333,22 +351,22 @@ __device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<
 
 // one link's momentum update: P_mu(x) -= coef proj(U_mu(x) S_mu(x)); returns
 // the kinetic norm of the updated momentum
-template <int GRP, class T, int ND>
+template <int GRP, class T, int ND, bool F2 = false>
 __device__ __forceinline__ double force_item(Geom const &g, Site<ND> const &st, int64_t s, int mu,
                                              LinkLoad<GRP, T, ND> const &ld, T *__restrict__ P, T coef)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
-	E S = staple<GRP, T, ND>(g, st, s, mu, ld);
-	E W = Gp::mul(ld(mu, s), S);
+	E S = staple<GRP, T, ND, F2>(g, st, s, mu, ld);
+	E W = Prod<GRP, T, F2>::mul(ld(mu, s), S);
 	T f[Gp::NA], p[Gp::NA];
 	Gp::proj(W, f);
 	auto Pv = comp<T, Gp::NA>(P, g.V, mu);
-	Pv.load(s, p);
+	Pv.template load<CACHE_STREAM>(s, p);
 #pragma unroll
 	for (int k = 0; k < Gp::NA; ++k)
 		p[k] -= coef * f[k];
-	Pv.store(s, p);
+	Pv.template store<CACHE_STREAM>(s, p);
 	return double(Gp::kin(p));
 }
 
@@ -382,7 +400,7 @@ struct TileSpec
 	int ntiles; // tiles in the lattice
 };
 
-template <int GRP, class T, int ND, int NT, int MINB>
+template <int GRP, class T, int ND, int NT, int MINB, bool F2 = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_tiled(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin)
 {
@@ -413,7 +431,7 @@ __global__ void __launch_bounds__(NT, MINB)
 			int64_t s = eo_of<ND>(g, st);
 #pragma unroll 1
 			for (int mu = 0; mu < ND; ++mu)
-				acc += force_item<GRP, T, ND>(g, st, s, mu, ld, P, coef);
+				acc += force_item<GRP, T, ND, F2>(g, st, s, mu, ld, P, coef);
 		}
 	}
 	if (kin.result)
@@ -973,15 +991,26 @@ template <int GRP, class T, int ND> struct Ops
 		int lt[4]; // log2 tile extents
 		int threads, minb;
 		char const *name;
+		bool f2 = false; // packed FP32x2 products (SU(3) float only)
 	};
-	static int n_force_variants() { return ND == 4 ? 8 : 2; }
+	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
+	static int n_force_variants() { return ND == 4 ? (kF2 ? 14 : 11) : 2; }
 	static ForceVariant force_variant(int v)
 	{
-		static const ForceVariant t[8] = {
-		    {0, {0, 0, 0, 0}, 256, 1, "eo-order/256thr/1blk"},   {0, {0, 0, 0, 0}, 256, 2, "eo-order/256thr/2blk"},
-		    {1, {2, 2, 2, 2}, 256, 1, "tile4x4x4x4/256thr/1blk"}, {1, {2, 2, 2, 2}, 256, 2, "tile4x4x4x4/256thr/2blk"},
-		    {1, {1, 2, 2, 2}, 128, 3, "tile2x4x4x4/128thr/3blk"}, {1, {1, 2, 2, 2}, 128, 4, "tile2x4x4x4/128thr/4blk"},
-		    {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk"}, {1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk"}};
+		static const ForceVariant t[11] = {
+		    {0, {0, 0, 0, 0}, 256, 1, "eo-order/256thr/1blk"},    {0, {0, 0, 0, 0}, 256, 2, "eo-order/256thr/2blk"},
+		    {1, {2, 2, 2, 2}, 256, 1, "tile4x4x4x4/256thr/1blk"},  {1, {2, 2, 2, 2}, 256, 2, "tile4x4x4x4/256thr/2blk"},
+		    {1, {1, 2, 2, 2}, 128, 3, "tile2x4x4x4/128thr/3blk"},  {1, {1, 2, 2, 2}, 128, 4, "tile2x4x4x4/128thr/4blk"},
+		    {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk"},  {1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk"},
+		    {1, {1, 1, 1, 3}, 128, 4, "tile2x2x2x8/128thr/4blk"},  {1, {1, 1, 2, 4}, 128, 4, "tile2x2x4x16/128thr/4blk"},
+		    {1, {0, 1, 2, 4}, 128, 4, "tile1x2x4x16/128thr/4blk"}};
+		if (v >= 11)
+		{
+			static const ForceVariant f[3] = {{1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk/f32x2", true},
+			                                  {1, {1, 1, 2, 3}, 128, 3, "tile2x2x4x8/128thr/3blk/f32x2", true},
+			                                  {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk/f32x2", true}};
+			return f[v - 11];
+		}
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1028,7 +1057,19 @@ template <int GRP, class T, int ND> struct Ops
 			}
 			int64_t cap = int64_t(c.num_sms) * fv.minb;
 			unsigned b = unsigned(ts.ntiles < cap ? ts.ntiles : cap);
-			if (fv.threads == 256 && fv.minb == 1)
+			if (fv.f2)
+			{
+				if constexpr (kF2)
+				{
+					if (fv.threads == 128 && fv.minb == 4)
+						k_momentum_step_tiled<GRP, T, 4, 128, 4, true><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+					else if (fv.threads == 128)
+						k_momentum_step_tiled<GRP, T, 4, 128, 3, true><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+					else
+						k_momentum_step_tiled<GRP, T, 4, 256, 2, true><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				}
+			}
+			else if (fv.threads == 256 && fv.minb == 1)
 				k_momentum_step_tiled<GRP, T, 4, 256, 1><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
 			else if (fv.threads == 256 && fv.minb == 2)
 				k_momentum_step_tiled<GRP, T, 4, 256, 2><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
@@ -1050,6 +1091,9 @@ template <int GRP, class T, int ND> struct Ops
 	// momenta are rewritten unchanged); not while the stream is capturing
 	static int choose_force(Field &P, Field const &U)
 	{
+		int ov = force_override();
+		if (ov >= 0 && ov < n_force_variants() && force_variant_valid(U.geom, ov))
+			return ov;
 		std::string key = force_key(U);
 		int v = tuned_variant(key);
 		if (v >= 0)

@@ -173,6 +173,84 @@ inline int64_t eo_index_host(Geom const &g, int64_t r)
 }
 
 // ---------------------------------------------------------------------------
+// cache-policy loads/stores: links are re-read by neighbouring sites (keep
+// them in L1), momenta are touched once per kernel (stream them past L1)
+// ---------------------------------------------------------------------------
+enum CachePolicy
+{
+	CACHE_DEFAULT = 0,
+	CACHE_KEEP = 1,   // read-only path, L1 evict_last
+	CACHE_STREAM = 2, // evict-first streaming
+};
+
+template <int CP> __device__ __forceinline__ float4 ld4(float4 const *p)
+{
+	if constexpr (CP == CACHE_KEEP)
+	{
+		float4 r;
+		asm volatile("ld.global.nc.L1::evict_last.v4.f32 {%0,%1,%2,%3}, [%4];"
+		             : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+		             : "l"(p));
+		return r;
+	}
+	else if constexpr (CP == CACHE_STREAM)
+		return __ldcs(p);
+	else
+		return *p;
+}
+template <int CP> __device__ __forceinline__ float2 ld2(float2 const *p)
+{
+	if constexpr (CP == CACHE_KEEP)
+	{
+		float2 r;
+		asm volatile("ld.global.nc.L1::evict_last.v2.f32 {%0,%1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+		return r;
+	}
+	else if constexpr (CP == CACHE_STREAM)
+		return __ldcs(p);
+	else
+		return *p;
+}
+template <int CP> __device__ __forceinline__ float ld1(float const *p)
+{
+	if constexpr (CP == CACHE_KEEP)
+		return __ldg(p);
+	else if constexpr (CP == CACHE_STREAM)
+		return __ldcs(p);
+	else
+		return *p;
+}
+template <int CP> __device__ __forceinline__ double2 ld2d(double2 const *p)
+{
+	if constexpr (CP == CACHE_KEEP)
+	{
+		double2 r;
+		asm volatile("ld.global.nc.L1::evict_last.v2.f64 {%0,%1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+		return r;
+	}
+	else if constexpr (CP == CACHE_STREAM)
+		return __ldcs(p);
+	else
+		return *p;
+}
+template <int CP> __device__ __forceinline__ double ld1d(double const *p)
+{
+	if constexpr (CP == CACHE_KEEP)
+		return __ldg(p);
+	else if constexpr (CP == CACHE_STREAM)
+		return __ldcs(p);
+	else
+		return *p;
+}
+template <int CP, class V> __device__ __forceinline__ void stv(V *p, V v)
+{
+	if constexpr (CP == CACHE_STREAM)
+		__stcs(p, v);
+	else
+		*p = v;
+}
+
+// ---------------------------------------------------------------------------
 // structure-of-arrays planes
 // ---------------------------------------------------------------------------
 template <class T, int NR> struct Soa;
@@ -181,13 +259,14 @@ template <int NR> struct Soa<float, NR>
 {
 	static constexpr int N4 = NR / 4;
 	static constexpr int R = NR % 4;
+	template <int CP = CACHE_DEFAULT>
 	__device__ __forceinline__ static void load(float const *__restrict__ base, int64_t V, int64_t s, float *v)
 	{
 		float4 const *p4 = reinterpret_cast<float4 const *>(base);
 #pragma unroll
 		for (int k = 0; k < N4; ++k)
 		{
-			float4 t = p4[k * V + s];
+			float4 t = ld4<CP>(p4 + (k * V + s));
 			v[4 * k] = t.x;
 			v[4 * k + 1] = t.y;
 			v[4 * k + 2] = t.z;
@@ -196,55 +275,58 @@ template <int NR> struct Soa<float, NR>
 		float const *tail = base + int64_t(4 * N4) * V;
 		if constexpr (R >= 2)
 		{
-			float2 t = reinterpret_cast<float2 const *>(tail)[s];
+			float2 t = ld2<CP>(reinterpret_cast<float2 const *>(tail) + s);
 			v[4 * N4] = t.x;
 			v[4 * N4 + 1] = t.y;
 			tail += 2 * V;
 		}
 		if constexpr (R & 1)
-			v[NR - 1] = tail[s];
+			v[NR - 1] = ld1<CP>(tail + s);
 	}
+	template <int CP = CACHE_DEFAULT>
 	__device__ __forceinline__ static void store(float *__restrict__ base, int64_t V, int64_t s, float const *v)
 	{
 		float4 *p4 = reinterpret_cast<float4 *>(base);
 #pragma unroll
 		for (int k = 0; k < N4; ++k)
-			p4[k * V + s] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+			stv<CP>(p4 + (k * V + s), make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]));
 		float *tail = base + int64_t(4 * N4) * V;
 		if constexpr (R >= 2)
 		{
-			reinterpret_cast<float2 *>(tail)[s] = make_float2(v[4 * N4], v[4 * N4 + 1]);
+			stv<CP>(reinterpret_cast<float2 *>(tail) + s, make_float2(v[4 * N4], v[4 * N4 + 1]));
 			tail += 2 * V;
 		}
 		if constexpr (R & 1)
-			tail[s] = v[NR - 1];
+			stv<CP>(tail + s, v[NR - 1]);
 	}
 };
 
 template <int NR> struct Soa<double, NR>
 {
 	static constexpr int N2 = NR / 2;
+	template <int CP = CACHE_DEFAULT>
 	__device__ __forceinline__ static void load(double const *__restrict__ base, int64_t V, int64_t s, double *v)
 	{
 		double2 const *p2 = reinterpret_cast<double2 const *>(base);
 #pragma unroll
 		for (int k = 0; k < N2; ++k)
 		{
-			double2 t = p2[k * V + s];
+			double2 t = ld2d<CP>(p2 + (k * V + s));
 			v[2 * k] = t.x;
 			v[2 * k + 1] = t.y;
 		}
 		if constexpr (NR & 1)
-			v[NR - 1] = (base + int64_t(2 * N2) * V)[s];
+			v[NR - 1] = ld1d<CP>(base + int64_t(2 * N2) * V + s);
 	}
+	template <int CP = CACHE_DEFAULT>
 	__device__ __forceinline__ static void store(double *__restrict__ base, int64_t V, int64_t s, double const *v)
 	{
 		double2 *p2 = reinterpret_cast<double2 *>(base);
 #pragma unroll
 		for (int k = 0; k < N2; ++k)
-			p2[k * V + s] = make_double2(v[2 * k], v[2 * k + 1]);
+			stv<CP>(p2 + (k * V + s), make_double2(v[2 * k], v[2 * k + 1]));
 		if constexpr (NR & 1)
-			(base + int64_t(2 * N2) * V)[s] = v[NR - 1];
+			stv<CP>(base + int64_t(2 * N2) * V + s, v[NR - 1]);
 	}
 };
 
@@ -253,8 +335,14 @@ template <class T, int NR> struct View
 {
 	T *base;
 	int64_t V;
-	__device__ __forceinline__ void load(int64_t s, T *v) const { Soa<T, NR>::load(base, V, s, v); }
-	__device__ __forceinline__ void store(int64_t s, T const *v) const { Soa<T, NR>::store(base, V, s, v); }
+	template <int CP = CACHE_DEFAULT> __device__ __forceinline__ void load(int64_t s, T *v) const
+	{
+		Soa<T, NR>::template load<CP>(base, V, s, v);
+	}
+	template <int CP = CACHE_DEFAULT> __device__ __forceinline__ void store(int64_t s, T const *v) const
+	{
+		Soa<T, NR>::template store<CP>(base, V, s, v);
+	}
 };
 
 template <class T, int NR> __host__ __device__ __forceinline__ View<T, NR> comp(T *base, int64_t V, int c)

@@ -31,6 +31,12 @@ void set_tuned_variant(std::string const &key, int variant, std::string const &r
 	registry()[key] = {variant, report};
 }
 
+namespace {
+int g_force_override = -1;
+}
+int force_override() { return g_force_override; }
+void set_force_override(int v) { g_force_override = v; }
+
 bool autotune_enabled()
 {
 	char const *e = std::getenv("MESH_AUTOTUNE");
@@ -57,4 +63,12 @@ extern "C" size_t mesh_tune_report(char *buf, size_t cap)
 		buf[n] = '\0';
 	}
 	return r.size() + 1;
+}
+
+extern "C" int mesh_tune_force_variant(int variant)
+{
+	if (variant < -1 || variant >= 64)
+		return MESH_ERR_ARG;
+	meshgb::set_force_override(variant);
+	return MESH_OK;
 }

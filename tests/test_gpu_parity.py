@@ -140,8 +140,9 @@ def test_plaquette_action_vs_oracle(ctx, oracle, g, p, dims):
     ref = oracle.plaquette(g, 2, dims, U64)
     assert mg.plaquette(U) == pytest.approx(ref, rel=1e-13, abs=1e-15) if p == 2 else \
         mg.plaquette(U) == pytest.approx(ref, abs=1e-6)
-    U_hot = gauge(ctx, g, p, dims, oracle.random_gauge(g, p, dims, 8))
-    assert mg.plaquette(U_hot) == pytest.approx(oracle.plaquette(g, 2, dims, oracle.random_gauge(g, 2, dims, 8)),
+    hot = oracle.random_gauge(g, p, dims, 8)
+    U_hot = gauge(ctx, g, p, dims, hot)
+    assert mg.plaquette(U_hot) == pytest.approx(oracle.plaquette(g, 2, dims, hot.astype(np.float64)),
                                                 abs=1e-14 if p == 2 else 1e-6)
     S = oracle.wilson_action(g, 2, dims, U64, BETA[g])
     assert mg.wilson_action(U, BETA[g]) == pytest.approx(S, rel=1e-12 if p == 2 else 1e-5)
@@ -173,6 +174,25 @@ def test_staples_force_evolve_reunit_vs_oracle(ctx, oracle, g, p):
     assert rel(Uw.export(), oracle.reunitize(g, 2, dims, U64 * 1.0005)) < tol(p)
     U = gauge(ctx, g, p, dims, U64.astype(dt))
     mg.momentum_step(P, U, BETA[g], 0.05)
+    assert rel(P.export(), oracle.momentum_step(g, 2, dims, U64, P64, BETA[g], 0.05)) < tol(p)
+
+
+@pytest.mark.parametrize("variant", list(range(14)))
+@pytest.mark.parametrize("g,p", [(3, 1), (3, 2), (2, 1), (1, 1)])
+def test_every_force_launch_variant_vs_oracle(ctx, oracle, g, p, variant):
+    """each launch variant the autotuner can choose (even/odd order, 4D tiles,
+    packed FP32x2 products) computes the same momentum step"""
+    dims = [8, 8, 8, 16]
+    U64 = thermal(oracle, g, dims, ntraj=1)
+    P64 = oracle.random_momenta(g, 2, dims, 9, 0)
+    dt = mg.real_dtype(p)
+    U = gauge(ctx, g, p, dims, U64.astype(dt))
+    P = momenta(ctx, g, p, dims, P64.astype(dt))
+    try:
+        mg.force_variant(variant)
+        mg.momentum_step(P, U, BETA[g], 0.05)
+    finally:
+        mg.force_variant(-1)
     assert rel(P.export(), oracle.momentum_step(g, 2, dims, U64, P64, BETA[g], 0.05)) < tol(p)
 
 
@@ -244,7 +264,9 @@ def test_device_momenta_match_oracle_stream(ctx, oracle, g, p):
     assert rel(P.export(), ref) < (1e-14 if p == 2 else 2e-6)
     U = mg.GaugeField(ctx, g, p, mg.Grid(dims)).random(78)
     ref = oracle.random_gauge(g, p, dims, 78)
-    assert rel(U.export(), ref) < (1e-13 if p == 2 else 5e-6)
+    # FP32 Gram-Schmidt amplifies last-ulp differences of the transcendental
+    # functions in Box-Muller (device sincospif/logf vs host libm)
+    assert rel(U.export(), ref) < (1e-13 if p == 2 else 1e-4)
 
 
 def test_graph_replay_equals_eager(ctx):
