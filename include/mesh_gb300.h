@@ -61,6 +61,7 @@ extern "C" {
 typedef struct mesh_ctx_s *mesh_ctx;
 typedef struct mesh_field_s *mesh_field;
 typedef struct mesh_hmc_s *mesh_hmc;
+typedef struct mesh_landau_fa_s *mesh_landau_fa;
 
 /* ---- library ------------------------------------------------------------ */
 /* last error message of the calling thread (valid until the next call) */
@@ -225,6 +226,58 @@ int mesh_landau_or(mesh_field U, mesh_field g, double omega, double tol, int max
                    int *sweeps, double *theta);
 /* U <- g U g^dagger(x+mu) for all mu (apply a gauge transform) */
 int mesh_gauge_transform(mesh_field U, mesh_field g);
+
+/* ---- Fourier-accelerated Landau gauge fixing (no reference counterpart;
+ * the reference's FFT helpers, src/lattice/fft.h:36-61, wrap FFTW on the host
+ * and are unused) -------------------------------------------------------------
+ * Steepest descent with a spectral multiplier (Davies et al., Phys. Rev. D 37
+ * (1988) 1581): g <- reunit(exp(-F^-1[m(p) F[Delta]]/V) g), Delta the lattice
+ * divergence of the gauge-fixed links. g and U are FP64; the transform is an
+ * FP32 FFT (it only shapes the step); theta is FP64. Extents must be
+ * 2,4,6,8,12,16,24 or 32. The workspace borrows U (keep it alive). */
+int mesh_landau_fa_create(mesh_field U, mesh_landau_fa *out);
+int mesh_landau_fa_destroy(mesh_landau_fa h);
+/* m(p) = alpha * p2max / phat^2(p), 0 at p = 0 (phat^2 = sum 4 sin^2(pi n/L)) */
+int mesh_landau_fa_set_plain(mesh_landau_fa h, double alpha);
+/* m(p) = exp(table) sampled on n points uniform in log phat^2 */
+int mesh_landau_fa_set_table(mesh_landau_fa h, const float *log_mult, int n, double log_p2_lo, double log_p2_hi);
+/* learned multiplier: log m = MLP(log phat^2 - log p2max, 5(beta-6),
+ * (log10 theta + 7)/5), width 32 or 64, re-evaluated before every step
+ * (BF16 inference when bf16 != 0) */
+int mesh_landau_fa_set_mlp(mesh_landau_fa h, const float *params, int width, double beta, int bf16);
+/* smallest non-zero and largest phat^2 of the lattice */
+int mesh_landau_fa_p2range(mesh_landau_fa h, double *p2min, double *p2max);
+/* theta_ref of g (FP64) */
+int mesh_landau_fa_theta(mesh_landau_fa h, mesh_field g, double *theta);
+/* one step in place; theta of g before the step */
+int mesh_landau_fa_step(mesh_landau_fa h, mesh_field g, double *theta_before);
+/* steps until theta < tol; a step that does not lower theta is undone and
+ * or_sweeps overrelaxation sweeps (omega) run instead (the fallback) */
+int mesh_landau_fa_run(mesh_landau_fa h, mesh_field g, double tol, int max_iter, double omega, int or_sweeps,
+                       int *iters, int *fallbacks, double *theta);
+/* response of the momentum modes to a probe step (multiplier probe_alpha
+ * p2max/phat^2), per bin of log phat^2: mean phat^2, lambda = effective
+ * contraction rate per unit multiplier, weight, count; theta of g */
+int mesh_landau_fa_probe(mesh_landau_fa h, mesh_field g, double probe_alpha, int nbins, double *p2_mean,
+                         double *lambda, double *weight, double *count, double *theta);
+
+/* ---- lattice FFT (fft_all, src/lattice/fft.h:55-58) ----------------------------
+ * unnormalised FFT over every axis of nf complex FP32 fields, host array
+ * [nf][V] interleaved (re, im), lexicographic sites; sign -1 forward
+ * (e^{-2 pi i k x/L}), +1 backward */
+int mesh_lattice_fft(mesh_ctx ctx, int nd, const int32_t *dims, int nf, float *data, int sign);
+
+/* ---- the learned multiplier's network (3 -> width -> width -> 1 tanh MLP) --
+ * params (float): W1[w][3] b1[w] W2[w][w] b2[w] W3[w] b3; host arrays;
+ * computed on the context's device */
+int mesh_mlp_nparams(int width);
+int mesh_mlp_forward(mesh_ctx ctx, int n, const float *x, const float *params, int width, int bf16, float *y);
+/* mean squared error over n samples and its gradient (backward pass) */
+int mesh_mlp_grad(mesh_ctx ctx, int n, const float *x, const float *t, const float *params, int width, double *loss,
+                  float *grad);
+/* Adam training in shuffled minibatches, params updated in place */
+int mesh_mlp_train(mesh_ctx ctx, int n, const float *x, const float *t, float *params, int width, int epochs,
+                   int batch, float lr, uint64_t seed, float *loss_per_epoch);
 
 #ifdef __cplusplus
 }

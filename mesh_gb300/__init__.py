@@ -106,6 +106,23 @@ SIGNATURES = {
     "mesh_landau_cg": (_I, [_P, _P, _I, _D, _IP, _DP]),
     "mesh_landau_or": (_I, [_P, _P, _D, _D, _I, _I, _IP, _DP]),
     "mesh_gauge_transform": (_I, [_P, _P]),
+    "mesh_landau_fa_create": (_I, [_P, _PP]),
+    "mesh_landau_fa_destroy": (_I, [_P]),
+    "mesh_landau_fa_set_plain": (_I, [_P, _D]),
+    "mesh_landau_fa_set_table": (_I, [_P, C.POINTER(C.c_float), _I, _D, _D]),
+    "mesh_landau_fa_set_mlp": (_I, [_P, C.POINTER(C.c_float), _I, _D, _I]),
+    "mesh_landau_fa_p2range": (_I, [_P, _DP, _DP]),
+    "mesh_landau_fa_theta": (_I, [_P, _P, _DP]),
+    "mesh_landau_fa_step": (_I, [_P, _P, _DP]),
+    "mesh_landau_fa_run": (_I, [_P, _P, _D, _I, _D, _I, _IP, _IP, _DP]),
+    "mesh_landau_fa_probe": (_I, [_P, _P, _D, _I, _DP, _DP, _DP, _DP, _DP]),
+    "mesh_lattice_fft": (_I, [_P, _I, _I32P, _I, C.POINTER(C.c_float), _I]),
+    "mesh_mlp_nparams": (_I, [_I]),
+    "mesh_mlp_forward": (_I, [_P, _I, C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _I, C.POINTER(C.c_float)]),
+    "mesh_mlp_grad": (_I, [_P, _I, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _DP,
+                           C.POINTER(C.c_float)]),
+    "mesh_mlp_train": (_I, [_P, _I, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _I, _I,
+                            C.c_float, _U64, C.POINTER(C.c_float)]),
 }
 
 _lib = None
@@ -512,3 +529,124 @@ class Landau:
         if rc != 0 and (rc != 6 or raise_on_noconv):
             _chk(rc)
         return s.value, th.value
+
+
+# ---- Fourier-accelerated Landau fixing, FFT, MLP -------------------------------
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class LandauFA:
+    """Fourier-accelerated steepest descent for Landau gauge on FP64 links,
+    with the plain multiplier alpha p2max/p^2 or the learned MLP multiplier."""
+
+    def __init__(self, U: Field):
+        self.U = U
+        h = C.c_void_p()
+        _chk(load().mesh_landau_fa_create(U.h, C.byref(h)))
+        self.h = h
+
+    def set_plain(self, alpha: float):
+        _chk(load().mesh_landau_fa_set_plain(self.h, alpha))
+
+    def set_table(self, log_mult, log_p2_lo: float, log_p2_hi: float):
+        a = np.ascontiguousarray(log_mult, dtype=np.float32)
+        _chk(load().mesh_landau_fa_set_table(self.h, _fp(a), len(a), log_p2_lo, log_p2_hi))
+
+    def set_mlp(self, params, width: int, beta: float, bf16: bool = True):
+        a = np.ascontiguousarray(params, dtype=np.float32)
+        _chk(load().mesh_landau_fa_set_mlp(self.h, _fp(a), width, beta, 1 if bf16 else 0))
+
+    def p2range(self):
+        a, b = C.c_double(), C.c_double()
+        _chk(load().mesh_landau_fa_p2range(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def theta(self, g: Field) -> float:
+        t = C.c_double()
+        _chk(load().mesh_landau_fa_theta(self.h, g.h, C.byref(t)))
+        return t.value
+
+    def step(self, g: Field) -> float:
+        t = C.c_double()
+        _chk(load().mesh_landau_fa_step(self.h, g.h, C.byref(t)))
+        return t.value
+
+    def run(self, g: Field, tol=1e-12, max_iter=100000, omega=1.7, or_sweeps=10, raise_on_noconv=False):
+        it, fb, th = C.c_int(), C.c_int(), C.c_double()
+        rc = load().mesh_landau_fa_run(self.h, g.h, tol, max_iter, omega, or_sweeps, C.byref(it), C.byref(fb),
+                                       C.byref(th))
+        if rc != 0 and (rc != 6 or raise_on_noconv):
+            _chk(rc)
+        return it.value, fb.value, th.value
+
+    def probe(self, g: Field, probe_alpha: float, nbins: int = 64):
+        p2, lam, w, cnt = (np.zeros(nbins) for _ in range(4))
+        th = C.c_double()
+        _chk(load().mesh_landau_fa_probe(self.h, g.h, probe_alpha, nbins, p2.ctypes.data_as(_DP),
+                                         lam.ctypes.data_as(_DP), w.ctypes.data_as(_DP), cnt.ctypes.data_as(_DP),
+                                         C.byref(th)))
+        return {"p2": p2, "lambda": lam, "weight": w, "count": cnt, "theta": th.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mesh_landau_fa_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def lattice_fft(ctx: Context, dims, data, sign: int) -> np.ndarray:
+    """data: complex64 array (nf, V) in lexicographic order; returns the
+    unnormalised transform over all axes (sign -1 forward, +1 backward)."""
+    a = np.ascontiguousarray(np.asarray(data, dtype=np.complex64))
+    nf = a.shape[0] if a.ndim == 2 else 1
+    f = a.view(np.float32)
+    _chk(load().mesh_lattice_fft(ctx.h, len(dims), _dims(dims), nf, _fp(f), sign))
+    return a
+
+
+def mlp_nparams(width: int) -> int:
+    return load().mesh_mlp_nparams(width)
+
+
+def mlp_forward(ctx: Context, x, params, width: int, bf16: bool = False) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    y = np.zeros(x.shape[0], dtype=np.float32)
+    _chk(load().mesh_mlp_forward(ctx.h, x.shape[0], _fp(x), _fp(p), width, 1 if bf16 else 0, _fp(y)))
+    return y
+
+
+def mlp_grad(ctx: Context, x, t, params, width: int):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    g = np.zeros(mlp_nparams(width), dtype=np.float32)
+    loss = C.c_double()
+    _chk(load().mesh_mlp_grad(ctx.h, x.shape[0], _fp(x), _fp(t), _fp(p), width, C.byref(loss), _fp(g)))
+    return loss.value, g
+
+
+def mlp_train(ctx: Context, x, t, params, width: int, epochs: int, batch: int = 1024, lr: float = 1e-3,
+              seed: int = 0):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32).copy()
+    losses = np.zeros(max(epochs, 1), dtype=np.float32)
+    _chk(load().mesh_mlp_train(ctx.h, x.shape[0], _fp(x), _fp(t), _fp(p), width, epochs, batch, lr, seed,
+                               _fp(losses)))
+    return p, losses[:epochs]
+
+
+def mlp_init(width: int, seed: int = 0) -> np.ndarray:
+    """Glorot-style initial parameters in the library's layout."""
+    rng = np.random.default_rng(seed)
+    w = width
+    parts = [rng.normal(0, np.sqrt(1 / 3), (w, 3)), np.zeros(w), rng.normal(0, np.sqrt(1 / w), (w, w)), np.zeros(w),
+             rng.normal(0, np.sqrt(1 / w), w), np.zeros(1)]
+    return np.concatenate([p.ravel() for p in parts]).astype(np.float32)

@@ -13,11 +13,6 @@
 
 using namespace meshgb;
 
-struct mesh_ctx_s
-{
-	Context c;
-};
-
 namespace {
 void teardown_ctx(Context &c)
 {
@@ -43,38 +38,21 @@ void release_ctx(Context *c)
 	}
 }
 } // namespace
-struct mesh_field_s
-{
-	Field f;
-};
 
 namespace {
 thread_local std::string g_err;
+} // namespace
 
+void meshgb::set_last_error(char const *msg) { g_err = msg; }
+
+namespace {
 int fail(int code, char const *msg)
 {
 	g_err = msg;
 	return code;
 }
 
-template <class F> int api(F f)
-{
-	try
-	{
-		f();
-		return MESH_OK;
-	}
-	catch (Error const &e)
-	{
-		g_err = e.what();
-		return e.code;
-	}
-	catch (std::exception const &e)
-	{
-		g_err = e.what();
-		return MESH_ERR_ARG;
-	}
-}
+template <class F> int api(F &&f) { return api_call(f); }
 
 Field &F(mesh_field h)
 {

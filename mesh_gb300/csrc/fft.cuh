@@ -21,7 +21,7 @@ namespace fft {
 
 // ---- compile-time sin/cos (Taylor series after reduction to [-pi/4, pi/4]) ----
 constexpr double kPi = 3.14159265358979323846264338327950288;
-constexpr double taylor_sin(double x)
+__host__ __device__ constexpr double taylor_sin(double x)
 {
 	double t = x, s = x;
 	for (int n = 1; n < 14; ++n)
@@ -31,7 +31,7 @@ constexpr double taylor_sin(double x)
 	}
 	return s;
 }
-constexpr double taylor_cos(double x)
+__host__ __device__ constexpr double taylor_cos(double x)
 {
 	double t = 1.0, s = 1.0;
 	for (int n = 1; n < 14; ++n)
@@ -42,7 +42,7 @@ constexpr double taylor_cos(double x)
 	return s;
 }
 // cos / sin of an angle in [0, pi], reduced to [0, pi/4]
-constexpr double cos_a(double a)
+__host__ __device__ constexpr double cos_a(double a)
 {
 	if (a > kPi / 2)
 		return -cos_a(kPi - a);
@@ -50,7 +50,7 @@ constexpr double cos_a(double a)
 		return taylor_sin(kPi / 2 - a);
 	return taylor_cos(a);
 }
-constexpr double sin_a(double a)
+__host__ __device__ constexpr double sin_a(double a)
 {
 	if (a > kPi / 2)
 		return sin_a(kPi - a);
@@ -59,14 +59,14 @@ constexpr double sin_a(double a)
 	return taylor_sin(a);
 }
 // cos and sin of 2 pi j / L for integers j, L
-constexpr double cos2pi(int j, int L)
+__host__ __device__ constexpr double cos2pi(int j, int L)
 {
 	j = ((j % L) + L) % L;
 	if (2 * j > L)
 		return cos2pi(L - j, L);
 	return cos_a(2.0 * kPi * double(j) / double(L));
 }
-constexpr double sin2pi(int j, int L)
+__host__ __device__ constexpr double sin2pi(int j, int L)
 {
 	j = ((j % L) + L) % L;
 	if (2 * j > L)
@@ -79,8 +79,8 @@ static_assert(sin2pi(1, 12) > 0.4999999999999 && sin2pi(1, 12) < 0.5000000000001
 template <int L, int SIGN> struct Twiddle
 {
 	// W^j = e^{SIGN 2 pi i j / L}
-	static constexpr float re(int j) { return float(cos2pi(j, L)); }
-	static constexpr float im(int j) { return float(double(SIGN) * sin2pi(j, L)); }
+	__host__ __device__ static constexpr float re(int j) { return float(cos2pi(j, L)); }
+	__host__ __device__ static constexpr float im(int j) { return float(double(SIGN) * sin2pi(j, L)); }
 };
 
 // compile-time loop: f(std::integral_constant<int, I>) for I in [B, E)

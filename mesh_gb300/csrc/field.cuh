@@ -135,6 +135,32 @@ inline OpsTable const &ops_for(int group, int prec, int nd)
 }
 inline OpsTable const &ops_for(Field const &f) { return ops_for(f.group, f.prec, f.nd); }
 
+// MLP inference on device arrays (mlp.cu): y[n] = MLP(x[n][3])
+void mlp_forward_device(Context &c, int n, float const *d_x, float const *d_params, int width, bool bf16, float *d_y);
+
+// the error message reported by mesh_last_error() (capi.cu)
+void set_last_error(char const *msg);
+
+// runs f, mapping exceptions to status codes (no exception crosses the ABI)
+template <class F> int api_call(F &&f)
+{
+	try
+	{
+		f();
+		return MESH_OK;
+	}
+	catch (Error const &e)
+	{
+		set_last_error(e.what());
+		return e.code;
+	}
+	catch (std::exception const &e)
+	{
+		set_last_error(e.what());
+		return MESH_ERR_ARG;
+	}
+}
+
 // HMC trajectory kernels (hmc.cu)
 void launch_metropolis(Context &c, HmcDev *dev, HmcRecordDev *hist, double const *S_cur, double const *K_old,
                        double const *S_new, double const *K_new, double *S_cur_out, double beta, double nplanes_V,
@@ -142,3 +168,13 @@ void launch_metropolis(Context &c, HmcDev *dev, HmcRecordDev *hist, double const
 void launch_copy_if(Context &c, void *dst, void const *src, size_t bytes, int const *flag);
 
 } // namespace meshgb
+
+// objects behind the C ABI handles
+struct mesh_ctx_s
+{
+	meshgb::Context c;
+};
+struct mesh_field_s
+{
+	meshgb::Field f;
+};
