@@ -603,7 +603,7 @@ class LandauFA:
 def lattice_fft(ctx: Context, dims, data, sign: int) -> np.ndarray:
     """data: complex64 array (nf, V) in lexicographic order; returns the
     unnormalised transform over all axes (sign -1 forward, +1 backward)."""
-    a = np.ascontiguousarray(np.asarray(data, dtype=np.complex64))
+    a = np.array(data, dtype=np.complex64, order="C", copy=True)
     nf = a.shape[0] if a.ndim == 2 else 1
     f = a.view(np.float32)
     _chk(load().mesh_lattice_fft(ctx.h, len(dims), _dims(dims), nf, _fp(f), sign))

@@ -19,7 +19,7 @@ BETA = {1: 2.0, 2: 2.5, 3: 6.0}
 
 
 def rel(a, b):
-    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    a, b = np.asarray(a), np.asarray(b)
     return float(np.max(np.abs(a - b)) / max(1e-300, float(np.max(np.abs(b)))))
 
 
@@ -61,10 +61,12 @@ def test_fa_step_vs_oracle(ctx, oracle, g):
     gt = mg.Lattice(ctx, g, mg.F64, mg.Grid(dims)).set_unit()
     g64 = oracle.unit_transform(g, 2, dims)
     mult = plain_mult(dims, 0.06)
-    for _ in range(3):
+    for k in range(3):
         th = fa.step(gt)
         th_ref, _ = oracle.landau_theta(g, 2, dims, U64, g64)
-        assert th == pytest.approx(th_ref, rel=1e-9)
+        # theta is FP64 on both sides; after the first step the two g differ
+        # at the FP32-FFT level, ~1e-7
+        assert th == pytest.approx(th_ref, rel=1e-12 if k == 0 else 1e-5)
         g64 = oracle.landau_fa_step(g, 2, dims, U64, g64, mult, 1.0)
         assert rel(gt.export(), g64) < 2e-5
     assert fa.theta(gt) == pytest.approx(oracle.landau_theta(g, 2, dims, U64, g64)[0], rel=1e-3)
