@@ -255,6 +255,9 @@ int mesh_landau_fa_step(mesh_landau_fa h, mesh_field g, double *theta_before);
  * or_sweeps overrelaxation sweeps (omega) run instead (the fallback) */
 int mesh_landau_fa_run(mesh_landau_fa h, mesh_field g, double tol, int max_iter, double omega, int or_sweeps,
                        int *iters, int *fallbacks, double *theta);
+/* trial step that leaves g unchanged (the current multiplier, or the plain
+ * one with alpha when alpha > 0): theta before and after */
+int mesh_landau_fa_trial(mesh_landau_fa h, mesh_field g, double alpha, double *theta_before, double *theta_after);
 /* response of the momentum modes to a probe step (multiplier probe_alpha
  * p2max/phat^2), per bin of log phat^2: mean phat^2, lambda = effective
  * contraction rate per unit multiplier, weight, count; theta of g */

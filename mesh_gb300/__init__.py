@@ -116,6 +116,7 @@ SIGNATURES = {
     "mesh_landau_fa_step": (_I, [_P, _P, _DP]),
     "mesh_landau_fa_run": (_I, [_P, _P, _D, _I, _D, _I, _IP, _IP, _DP]),
     "mesh_landau_fa_probe": (_I, [_P, _P, _D, _I, _DP, _DP, _DP, _DP, _DP]),
+    "mesh_landau_fa_trial": (_I, [_P, _P, _D, _DP, _DP]),
     "mesh_lattice_fft": (_I, [_P, _I, _I32P, _I, C.POINTER(C.c_float), _I]),
     "mesh_mlp_nparams": (_I, [_I]),
     "mesh_mlp_forward": (_I, [_P, _I, C.POINTER(C.c_float), C.POINTER(C.c_float), _I, _I, C.POINTER(C.c_float)]),
@@ -579,6 +580,13 @@ class LandauFA:
         if rc != 0 and (rc != 6 or raise_on_noconv):
             _chk(rc)
         return it.value, fb.value, th.value
+
+    def trial(self, g: Field, alpha: float = 0.0):
+        """theta before and after a step that leaves g unchanged (plain
+        multiplier alpha if alpha > 0, else the current one)"""
+        a, b = C.c_double(), C.c_double()
+        _chk(load().mesh_landau_fa_trial(self.h, g.h, alpha, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def probe(self, g: Field, probe_alpha: float, nbins: int = 64):
         p2, lam, w, cnt = (np.zeros(nbins) for _ in range(4))

@@ -420,6 +420,34 @@ int mesh_landau_fa_run(mesh_landau_fa_s *h, mesh_field gh, double tol, int max_i
 	});
 }
 
+// Trial step that leaves g unchanged: the current multiplier, or the plain
+// one with `alpha` when alpha > 0; returns theta before and after the step.
+int mesh_landau_fa_trial(mesh_landau_fa_s *h, mesh_field gh, double alpha, double *theta_before, double *theta_after)
+{
+	return fa_api([&] {
+		require(h != nullptr && gh != nullptr, "null argument");
+		Field &g = gh->f;
+		require(g.same_grid(*h->U) && g.group == h->U->group && g.prec == MESH_F64 && g.nstack == 1,
+		        "g must be an FP64 site field on U's grid", MESH_ERR_STATE);
+		DeviceGuard dg(h->ctx->device);
+		double th = h->theta(g, true);
+		Multiplier m = h->mult;
+		if (alpha > 0)
+		{
+			m.mode = 0;
+			m.alpha = float(alpha);
+		}
+		h->step_from_buf(g, h->g_trial, m, th);
+		Field trial = g;
+		trial.d = h->g_trial;
+		double th2 = h->theta(trial, false);
+		if (theta_before)
+			*theta_before = th;
+		if (theta_after)
+			*theta_after = th2;
+	});
+}
+
 // Response probe: Delta(g) -> F_old; trial step with the plain multiplier
 // scaled by `probe_alpha`; Delta(trial) -> F_new; per log-p^2 bin
 // lambda_b = sum (|F_old|^2 - Re<F_new,F_old>)/m0 / sum |F_old|^2.

@@ -78,33 +78,79 @@ def prepared_links(ctx, U_host, transform_seed):
     return U
 
 
-def collect(ctx, U, beta, alpha=PLAIN_ALPHA, probe_alpha=0.02, nbins=48, every=2, tol=1e-12, max_iter=400):
-    """Probe samples along a plain Fourier-accelerated run: rows of
-    (features..., log lambda, weight)."""
+NONLINEAR_THETA = 1e-2  # above: indefinite Hessian, steps chosen by trial
+ALPHAS = (0.01, 0.02, 0.04, 0.06, 0.08, 0.12)
+
+
+def measured_table(pr, p2min, p2max, gamma, n=256):
+    """log multiplier gamma/lambda on the table grid from a probe, the
+    contraction rate clipped to [0.02, 20] (p^2/p2max) and interpolated in
+    log p^2; None when the probe has no usable bin"""
+    ok = (pr["count"] > 0) & np.isfinite(pr["lambda"])
+    if not np.any(ok):
+        return None
+    p2 = pr["p2"][ok]
+    lam = np.clip(pr["lambda"][ok], 0.02 * p2 / p2max, 20.0 * p2 / p2max)
+    lo, hi = np.log(p2min) - 1e-3, np.log(p2max) + 1e-3
+    grid = np.linspace(lo, hi, n)
+    return np.interp(grid, np.log(p2), np.log(gamma / lam)).astype(np.float32), lo, hi
+
+
+def collect(ctx, U, beta, gamma=0.5, probe_alpha=0.02, nbins=32, every=3, tol=1e-12, max_iter=600):
+    """Samples along a data-collection run. theta > 1e-2: the best plain step
+    size of a trial line search, target log(alpha* p2max/p^2) for every bin;
+    theta <= 1e-2: probed contraction rates, target log(gamma/lambda), and the
+    run is driven by the measured multiplier (refreshed every `every` steps).
+    Rows: (3 features, target, regime) with regime 0 nonlinear, 1 linear."""
     fa = LandauFA(U)
-    fa.set_plain(alpha)
+    fa.mult_mode = 0
     p2min, p2max = fa.p2range()
     g = Lattice(U.ctx, 3, F64, U.grid).set_unit()
     rows = []
+    centers = np.exp(np.linspace(np.log(p2min), np.log(p2max), nbins))
     for it in range(max_iter):
-        if it % every == 0:
-            pr = fa.probe(g, probe_alpha, nbins)
-            ok = (pr["count"] > 0) & (pr["lambda"] > 0) & np.isfinite(pr["lambda"])
-            if np.any(ok):
-                f = features(np.log(pr["p2"][ok]) - np.log(p2max), beta, pr["theta"])
-                rows.append(np.column_stack([f, np.log(pr["lambda"][ok]), pr["weight"][ok]]))
-            if pr["theta"] < tol:
-                break
-        th = fa.step(g)
+        th = fa.theta(g)
         if th < tol:
             break
+        if th > NONLINEAR_THETA:
+            res = [(fa.trial(g, a)[1], a) for a in ALPHAS]
+            th_best, a_best = min(res)
+            f = features(np.log(centers) - np.log(p2max), beta, th)
+            rows.append(np.column_stack([f, np.log(a_best * p2max / centers), np.zeros(nbins)]))
+            fa.set_plain(a_best)
+            fa.mult_mode = 0
+            fa.step(g)
+            continue
+        if it % every == 0 or fa.mult_mode != 1:
+            pr = fa.probe(g, probe_alpha, nbins)
+            ok = (pr["count"] > 0) & np.isfinite(pr["lambda"])
+            lam = np.clip(pr["lambda"][ok], 0.02 * pr["p2"][ok] / p2max, 20.0 * pr["p2"][ok] / p2max)
+            f = features(np.log(pr["p2"][ok]) - np.log(p2max), beta, pr["theta"])
+            rows.append(np.column_stack([f, np.log(lam), np.ones(int(ok.sum()))]))
+            tab = measured_table(pr, p2min, p2max, gamma)
+            if tab is not None:
+                fa.set_table(*tab)
+                fa.mult_mode = 1
+        before, after = fa.trial(g)
+        if after < before:
+            fa.step(g)
+        else:
+            # step rejected: a few overrelaxation sweeps (the run's fallback)
+            Lnd = Landau(U)
+            Lnd.g = g
+            Lnd.overrelax(1.7, tol=0.0, max_sweeps=5, check_every=5)
+            fa.mult_mode = 0
     fa.close()
+    collect.last_iterations = it
     return np.concatenate(rows) if rows else np.zeros((0, 5))
 
 
 def train(ctx, data, gamma, epochs=150, batch=2048, lr=2e-3, seed=0):
+    """targets: nonlinear rows keep log(alpha* p2max/p^2); linear rows
+    become log(gamma/lambda)"""
     x = data[:, :3].astype(np.float32)
-    t = (np.log(gamma) - data[:, 3]).astype(np.float32)
+    lin = data[:, 4] > 0.5
+    t = np.where(lin, np.log(gamma) - data[:, 3], data[:, 3]).astype(np.float32)
     p0 = mlp_init(WIDTH, seed)
     params, losses = mlp_train(ctx, x, t, p0, WIDTH, epochs=epochs, batch=batch, lr=lr, seed=seed)
     return params, losses
@@ -173,11 +219,13 @@ def main():
         for k, (beta, Uh) in enumerate(cfgs):
             U = prepared_links(ctx, Uh, transform_seed=5000 + k)
             data.append(collect(ctx, U, beta))
+            print(json.dumps({"config": k, "beta": beta, "collect_iterations": collect.last_iterations,
+                              "rows": int(len(data[-1]))}), flush=True)
         data = np.concatenate(data)
         t_collect = time.time() - t0 - t_gen
         # damping: pick gamma on four training configurations
         best = None
-        for gamma in (0.5, 0.7, 0.85, 1.0):
+        for gamma in (0.3, 0.5, 0.7, 1.0):
             params, losses = train(ctx, data, gamma)
             tot = 0.0
             for k in range(4):
