@@ -9,11 +9,16 @@ Method (no counterpart in the reference; written for this library):
   effective rate lambda depends on the configuration (beta) and on how far
   the fixing has got (theta).
 * Training data: on HMC-generated SU(3) configurations with random gauge
-  transforms, plain descent runs to theta < 1e-12 and is probed along the way
-  (mesh_landau_fa_probe): a trial step with a small known multiplier gives
-  lambda per bin of log phat^2. Each bin is a sample
-  x = (log phat^2 - log p2max, 5 (beta - 6), (log10 theta + 7)/5),
-  target = log(gamma / lambda), gamma a damping factor.
+  transforms, descent runs to theta < 1e-12; every few steps a trial line
+  search (mesh_landau_fa_trial, g unchanged) over a two-parameter multiplier
+  family m(p) = alpha p2max/p^2 max(1, boost 4 p2min/p^2) (step size and a
+  boost of the slow long-wavelength modes) picks the member that lowers theta
+  most. Its log multiplier at a set of momenta is the target for the
+  features x = (log phat^2 - log p2max, 5 (beta - 6), (log10 theta + 7)/5).
+  The network amortises the line search: one inference per step instead of
+  a dozen trial steps. (mesh_landau_fa_probe, the per-momentum response, is
+  kept as a diagnostic: a residual-weighted response is not a safe per-mode
+  multiplier, as stiffer modes in a bin get over-stepped.)
 * Network: 3 -> 64 -> 64 -> 1 tanh MLP (FP32 weights), trained on the GPU by
   the library's own forward/backward/Adam kernels (mesh_mlp_train); used with
   BF16 inference (mesh_landau_fa_set_mlp) to rebuild the multiplier table
@@ -78,79 +83,66 @@ def prepared_links(ctx, U_host, transform_seed):
     return U
 
 
-NONLINEAR_THETA = 1e-2  # above: indefinite Hessian, steps chosen by trial
-ALPHAS = (0.01, 0.02, 0.04, 0.06, 0.08, 0.12)
+# multiplier family searched per step during data collection:
+#   m(p) = alpha * p2max/p^2 * max(1, boost * p2ref/p^2),  p2ref = 4 p2min
+ALPHAS = (0.03, 0.05, 0.08, 0.11)
+BOOSTS = (1.0, 2.0, 4.0)
+TABLE_N = 256
 
 
-def measured_table(pr, p2min, p2max, gamma, n=256):
-    """log multiplier gamma/lambda on the table grid from a probe, the
-    contraction rate clipped to [0.02, 20] (p^2/p2max) and interpolated in
-    log p^2; None when the probe has no usable bin"""
-    ok = (pr["count"] > 0) & np.isfinite(pr["lambda"])
-    if not np.any(ok):
-        return None
-    p2 = pr["p2"][ok]
-    lam = np.clip(pr["lambda"][ok], 0.02 * p2 / p2max, 20.0 * p2 / p2max)
+def family_table(alpha, boost, p2min, p2max, n=TABLE_N):
     lo, hi = np.log(p2min) - 1e-3, np.log(p2max) + 1e-3
-    grid = np.linspace(lo, hi, n)
-    return np.interp(grid, np.log(p2), np.log(gamma / lam)).astype(np.float32), lo, hi
+    lp = np.linspace(lo, hi, n)
+    p2 = np.exp(lp)
+    m = alpha * p2max / p2 * np.maximum(1.0, boost * 4.0 * p2min / p2)
+    return np.log(m).astype(np.float32), lo, hi
 
 
-def collect(ctx, U, beta, gamma=0.5, probe_alpha=0.02, nbins=32, every=3, tol=1e-12, max_iter=600):
-    """Samples along a data-collection run. theta > 1e-2: the best plain step
-    size of a trial line search, target log(alpha* p2max/p^2) for every bin;
-    theta <= 1e-2: probed contraction rates, target log(gamma/lambda), and the
-    run is driven by the measured multiplier (refreshed every `every` steps).
-    Rows: (3 features, target, regime) with regime 0 nonlinear, 1 linear."""
+def collect(ctx, U, beta, every=4, tol=1e-12, max_iter=1500, nbins=24):
+    """Samples along a data-collection run: every `every` steps a trial line
+    search over the multiplier family (alpha, boost) picks the member giving
+    the lowest theta after one step; its log multiplier at `nbins` momenta is
+    the target for features (log p^2/p2max, beta, theta). The run advances
+    with that member, overrelaxation sweeps when a step fails to lower theta.
+    Rows: (3 features, target)."""
     fa = LandauFA(U)
-    fa.mult_mode = 0
     p2min, p2max = fa.p2range()
     g = Lattice(U.ctx, 3, F64, U.grid).set_unit()
     rows = []
     centers = np.exp(np.linspace(np.log(p2min), np.log(p2max), nbins))
+    lnd = Landau(U)
+    lnd.g = g
+    it = 0
     for it in range(max_iter):
         th = fa.theta(g)
         if th < tol:
             break
-        if th > NONLINEAR_THETA:
-            res = [(fa.trial(g, a)[1], a) for a in ALPHAS]
-            th_best, a_best = min(res)
-            f = features(np.log(centers) - np.log(p2max), beta, th)
-            rows.append(np.column_stack([f, np.log(a_best * p2max / centers), np.zeros(nbins)]))
-            fa.set_plain(a_best)
-            fa.mult_mode = 0
-            fa.step(g)
-            continue
-        if it % every == 0 or fa.mult_mode != 1:
-            pr = fa.probe(g, probe_alpha, nbins)
-            ok = (pr["count"] > 0) & np.isfinite(pr["lambda"])
-            lam = np.clip(pr["lambda"][ok], 0.02 * pr["p2"][ok] / p2max, 20.0 * pr["p2"][ok] / p2max)
-            f = features(np.log(pr["p2"][ok]) - np.log(p2max), beta, pr["theta"])
-            rows.append(np.column_stack([f, np.log(lam), np.ones(int(ok.sum()))]))
-            tab = measured_table(pr, p2min, p2max, gamma)
-            if tab is not None:
-                fa.set_table(*tab)
-                fa.mult_mode = 1
+        if it % every == 0:
+            best = None
+            for a in ALPHAS:
+                for b in BOOSTS:
+                    fa.set_table(*family_table(a, b, p2min, p2max))
+                    after = fa.trial(g)[1]
+                    if best is None or after < best[0]:
+                        best = (after, a, b)
+            _, a, b = best
+            tab = family_table(a, b, p2min, p2max)
+            fa.set_table(*tab)
+            tgt = np.log(a * p2max / centers * np.maximum(1.0, b * 4.0 * p2min / centers))
+            rows.append(np.column_stack([features(np.log(centers) - np.log(p2max), beta, th), tgt]))
         before, after = fa.trial(g)
         if after < before:
             fa.step(g)
         else:
-            # step rejected: a few overrelaxation sweeps (the run's fallback)
-            Lnd = Landau(U)
-            Lnd.g = g
-            Lnd.overrelax(1.7, tol=0.0, max_sweeps=5, check_every=5)
-            fa.mult_mode = 0
+            lnd.overrelax(1.7, tol=0.0, max_sweeps=10, check_every=10)
     fa.close()
     collect.last_iterations = it
-    return np.concatenate(rows) if rows else np.zeros((0, 5))
+    return np.concatenate(rows) if rows else np.zeros((0, 4))
 
 
-def train(ctx, data, gamma, epochs=150, batch=2048, lr=2e-3, seed=0):
-    """targets: nonlinear rows keep log(alpha* p2max/p^2); linear rows
-    become log(gamma/lambda)"""
+def train(ctx, data, epochs=200, batch=1024, lr=2e-3, seed=0):
     x = data[:, :3].astype(np.float32)
-    lin = data[:, 4] > 0.5
-    t = np.where(lin, np.log(gamma) - data[:, 3], data[:, 3]).astype(np.float32)
+    t = data[:, 3].astype(np.float32)
     p0 = mlp_init(WIDTH, seed)
     params, losses = mlp_train(ctx, x, t, p0, WIDTH, epochs=epochs, batch=batch, lr=lr, seed=seed)
     return params, losses
@@ -223,22 +215,13 @@ def main():
                               "rows": int(len(data[-1]))}), flush=True)
         data = np.concatenate(data)
         t_collect = time.time() - t0 - t_gen
-        # damping: pick gamma on four training configurations
-        best = None
-        for gamma in (0.3, 0.5, 0.7, 1.0):
-            params, losses = train(ctx, data, gamma)
-            tot = 0.0
-            for k in range(4):
-                U = prepared_links(ctx, cfgs[k][1], transform_seed=7000 + k)
-                tot += solve(ctx, U, "learned", params, cfgs[k][0], max_iter=3000)["seconds"]
-            if best is None or tot < best[0]:
-                best = (tot, gamma, params, losses)
-        _, gamma, params, losses = best
-        np.savez(args.out, params=params, gamma=gamma, width=WIDTH, samples=len(data),
-                 final_loss=float(losses[-1]), configs=len(cfgs), lattice=args.L)
-        print(json.dumps({"samples": int(len(data)), "gamma": gamma, "final_loss": float(losses[-1]),
-                          "first_loss": float(losses[0]), "t_generate_s": t_gen, "t_collect_s": t_collect,
-                          "configs": len(cfgs)}))
+        params, losses = train(ctx, data)
+        np.savez(args.out, params=params, gamma=1.0, width=WIDTH, samples=len(data),
+                 final_loss=float(losses[-1]), first_loss=float(losses[0]), configs=len(cfgs), lattice=args.L,
+                 betas=betas)
+        print(json.dumps({"samples": int(len(data)), "final_loss": float(losses[-1]),
+                          "first_loss": float(losses[0]), "target_variance": float(np.var(data[:, 3])),
+                          "t_generate_s": t_gen, "t_collect_s": t_collect, "configs": len(cfgs)}))
     else:
         params, gamma = load_weights()
         seeds = np.arange(1, args.eval_configs + 1)
