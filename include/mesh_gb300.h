@@ -141,6 +141,29 @@ int mesh_field_norm2(mesh_field a, double *out);
 int mesh_plaquette(mesh_field U, double *out);
 /* Wilson action (1 - plaquette) * beta * Nd(Nd-1)/2 * V (utils.h:141-146) */
 int mesh_wilson_action(mesh_field U, double beta, double *out);
+
+/* Plaquette without any device allocation. No counterpart in the reference.
+ * For callers that cannot call cudaMalloc when they measure: applications
+ * that give all device memory to their own pool or arena at start-up and
+ * forbid later allocations, or that run under a memory cap where a context
+ * (mesh_ctx_create allocates reduction scratch, a stream and staging) cannot
+ * be made. They pass plain pointers: `links` is a device buffer on `device`
+ * holding a gauge field of (group, precision, nd, dims) in the library's
+ * device storage (what mesh_field_device_ptr returns for such a field).
+ * Same kernel and grid as mesh_plaquette, so the same value bit for bit.
+ * Its reduction scratch is a static device array inside the library of
+ * MESH_NOALLOC_MAX_BLOCKS partial sums (8 KiB); a launch that would need more
+ * blocks is refused with MESH_ERR_ARG (none does on devices of up to 256 SMs).
+ * The first call on a device does set-up (may create the device's primary
+ * context and load the library's kernels, then resolves the scratch
+ * address); make that call before any stream capture. Runs on `stream`
+ * (NULL: the legacy default stream) and synchronises it. The scratch is
+ * shared by all callers in the process: calls that overlap on one device
+ * (several host threads, or work still in flight on another stream) race and
+ * must be serialised by the caller. */
+#define MESH_NOALLOC_MAX_BLOCKS 1024
+int mesh_plaquette_noalloc(int device, int group, int precision, int nd, const int32_t *dims, const void *links,
+                           void *stream, double *out);
 /* S = staple sum for direction mu (stapleSum, utils.h:114-139); S is a
  * single-component group field on U's grid */
 int mesh_staple_sum(mesh_field S, mesh_field U, int mu);

@@ -82,6 +82,7 @@ SIGNATURES = {
     "mesh_field_norm2": (_I, [_P, _DP]),
     "mesh_plaquette": (_I, [_P, _DP]),
     "mesh_wilson_action": (_I, [_P, _D, _DP]),
+    "mesh_plaquette_noalloc": (_I, [_I, _I, _I, _I, _I32P, _P, _P, _DP]),
     "mesh_staple_sum": (_I, [_P, _P, _I]),
     "mesh_wilson_deriv": (_I, [_P, _P, _I, _D]),
     "mesh_reunitize": (_I, [_P]),
