@@ -48,6 +48,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattice", type=int, default=32,
                     help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
+    ap.add_argument("--workload", choices=["hmc", "batch", "landau"], default="hmc",
+                    help="hmc: the headline line; batch: 64 SU(2) replicas in one persistent launch against 64 "
+                         "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
+                         "(plain and learned multiplier)")
+    ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
     a = ap.parse_args()
     if a.lattice != 32:
         WORKLOAD["dims"] = [a.lattice] * 4
@@ -347,10 +352,131 @@ def run_ours(args):
     return 0
 
 
+BATCH = dict(name="su2_batch_64rep_L{8,12,16,24}_beta[2.2,2.6]_2lf_eps0.5_n16_mixed", replicas=64,
+             sizes=(8, 12, 16, 24), beta=(2.2, 2.6), seed=99, scheme="2lf", eps=0.5, substeps=16)
+
+
+def batch_workload():
+    """64 SU(2) replicas: extents uniform in {8,12,16,24}^4, beta uniform in
+    [2.2, 2.6], drawn with seed 99; replica r uses seed r + 1"""
+    import numpy as np
+
+    rng = np.random.default_rng(BATCH["seed"])
+    L = rng.choice(BATCH["sizes"], BATCH["replicas"])
+    betas = rng.uniform(*BATCH["beta"], BATCH["replicas"])
+    return [[int(x)] * 4 for x in L], betas, list(range(1, BATCH["replicas"] + 1))
+
+
+def run_batch(args):
+    """Batched replicas: aggregate link updates/s (sum over replicas of
+    4 V_r x 16 MD steps per trajectory) for the whole batch in one persistent
+    launch per trajectory step (CUDA-graph trajectory), against the same 64
+    chains run one after the other (64 separate launch sequences)."""
+    import numpy as np
+    import torch
+
+    import mesh_gb300 as mg
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    ctx = mg.Context(0, stream.cuda_stream)
+    dims, betas, seeds = batch_workload()
+    d = mg.make_deltas(BATCH["scheme"], BATCH["eps"], BATCH["substeps"])
+    links = sum(4 * int(np.prod(x)) for x in dims)
+    steps = args.steps
+    therm = min(args.therm, 20)
+    b = mg.HmcBatch(ctx, 2, mg.F32, dims, seeds)
+    b.cold_start()
+    b.run(betas, d, therm + args.warmup)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+
+    clocks = Clocks(0)
+    clocks.start()
+    t_batch = timed(lambda: b.run(betas, d, steps))
+    clk = clocks.stop()
+    acc = float(np.mean([b.history(r)["accept_history"][therm + args.warmup:].mean() for r in range(b.R)]))
+    plaq = b.plaquettes()
+    info = b.launch_info(len(d))
+    chains = []
+    for r in range(len(dims)):
+        h = mg.Hmc(ctx, 2, mg.F32, mg.Grid(dims[r]), seed=seeds[r])
+        h.cold_start()
+        h.run(float(betas[r]), d, therm + args.warmup)
+        chains.append(h)
+    t_sep = timed(lambda: [h.run(float(betas[r]), d, steps) for r, h in enumerate(chains)])
+    updates = links * BATCH["substeps"] * steps
+    bytes_per_update = 84  # SU(2) FP32: force |U|+2|P| = 40 B, link update 2|U|+|P| = 44 B per link
+    peak, _ = measured_peaks()
+    out = {"metric": "SU(2) batched replicas link-updates/s", "value": updates / t_batch, "unit": "link-updates/s",
+           "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": t_batch / steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": BATCH["name"], "replicas": len(dims), "links": links,
+                      "sites": links // 4, "step": "one trajectory of every replica",
+                      "start": f"cold, {therm} + {args.warmup} untimed trajectories",
+                      "l2": f"inputs larger than L2 (links {links * 16 / 1e6:.0f} MB)"},
+           "separate": {"value": updates / t_sep, "ms_per_step": t_sep / steps * 1e3,
+                        "what": "the same 64 chains, each its own CUDA-graph trajectory, one after the other"},
+           "speedup_vs_separate": t_sep / t_batch,
+           "effective_GBps": updates * bytes_per_update / t_batch / 1e9, "peak_GBps": peak,
+           "physics": {"acceptance": acc, "plaquette_mean": float(plaq.mean())},
+           "gpu_launches": info["launches_per_trajectory"] * steps, "grids": info, "clocks": clk}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_landau(args):
+    """Time to theta < 1e-12 from a Haar-random gauge transform of thermalised
+    SU(3) L^4 beta = 6.0 configurations: FP64 overrelaxation (omega 1.7) and
+    Fourier-accelerated steepest descent with the plain and the learned
+    spectral multiplier (overrelaxation fallback)."""
+    import numpy as np
+
+    import mesh_gb300 as mg
+    from mesh_gb300 import landau_learn as ll
+
+    ctx = mg.Context(0)
+    L = args.lattice
+    seeds = np.arange(1, args.configs + 1)
+    cfgs = ll.hmc_configs(ctx, L, [6.0] * len(seeds), seeds, args.therm, 1, 0)
+    params, _ = ll.load_weights()
+    rows = []
+    for k, (beta, Uh) in enumerate(cfgs):
+        for method in ("or", "plain", "learned"):
+            U = ll.prepared_links(ctx, Uh, transform_seed=5)
+            r = ll.solve(ctx, U, method, params, beta)
+            r["config"] = k
+            rows.append(r)
+    summ = {m: {"mean_seconds": float(np.mean([r["seconds"] for r in rows if r["method"] == m])),
+                "mean_iterations": float(np.mean([r["iterations"] for r in rows if r["method"] == m])),
+                "fallbacks": int(sum(r["fallbacks"] for r in rows if r["method"] == m))}
+            for m in ("or", "plain", "learned")}
+    out = {"metric": "Landau gauge fixing seconds to theta<1e-12", "value": summ["learned"]["mean_seconds"],
+           "unit": "s", "n_gpus": 1, "steps": len(cfgs), "higher_is_better": False, "dtype": "f64",
+           "data": "synthetic", "config": {"workload": f"su3_landau_{L}^4_beta6.0_or1.7_vs_fa", "lattice": [L] * 4,
+                                           "thermalisation": f"{args.therm} trajectories, seeds 1..{len(cfgs)}",
+                                           "transform": "Haar-random, seed 5"},
+           "summary": summ, "speedup_learned_vs_or": summ["or"]["mean_seconds"] / summ["learned"]["mean_seconds"],
+           "speedup_plain_fa_vs_or": summ["or"]["mean_seconds"] / summ["plain"]["mean_seconds"], "rows": rows}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "landau":
+        return run_landau(args)
     return run_ours(args)
 
 

@@ -367,6 +367,9 @@ template <class G> class Hmc
 	}
 	void randomizeGaugeField() { check(mesh_hmc_randomize(get())); }
 	void coldStart() { check(mesh_hmc_cold_start(get())); }
+	// checkpoint / resume (links, trajectory counter, seed)
+	void save(std::string const &path) const { check(mesh_hmc_save(get(), path.c_str())); }
+	void load(std::string const &path) { check(mesh_hmc_load(get(), path.c_str())); }
 	// generate momenta -> run a trajectory -> accept/reject -> measure
 	void runHmcUpdate(double beta, std::vector<double> const &deltas)
 	{
@@ -396,6 +399,33 @@ template <class G> class Hmc
 		std::printf("<exp(-dH)> = %.4f\n", mean(deltaH_history, [](double x) { return std::exp(-x); }));
 	}
 };
+
+// ---- configuration files (writeToFile/readFromFile, lattice.h:205-252;
+// readConfig, utils.h:188-219) -----------------------------------------------------
+template <class G> void writeToFile(std::string const &path, BasicField<G> const &a)
+{
+	check(mesh_field_save(a.get(), path.c_str()));
+}
+template <class G> void readFromFile(std::string const &path, BasicField<G> &a)
+{
+	check(mesh_field_load(a.get(), path.c_str()));
+}
+// a gauge field with the file's grid; throws on a group mismatch, and on a
+// grid mismatch when expected_grid is given
+template <class G> GaugeField<G> readConfig(std::string const &path, Grid const *expected_grid = nullptr)
+{
+	int kind = 0, group = 0, prec = 0, nd = 0, nstack = 0;
+	int32_t dims[4] = {0, 0, 0, 0};
+	check(mesh_config_info(path.c_str(), &kind, &group, &prec, &nd, dims, &nstack, nullptr, nullptr));
+	if (group != GaugeTraits<G>::group || prec != GaugeTraits<G>::precision || kind != MESH_GROUP)
+		throw std::runtime_error("group mismatch on load");
+	Grid grid(std::vector<int32_t>(dims, dims + nd));
+	if (expected_grid && !(*expected_grid == grid))
+		throw std::runtime_error("grid mismatch on load");
+	GaugeField<G> U(grid);
+	readFromFile(path, U);
+	return U;
+}
 
 // ---- Landau (landau.h) -------------------------------------------------------------
 template <class G> struct Landau

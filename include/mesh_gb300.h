@@ -106,6 +106,18 @@ size_t mesh_field_host_bytes(mesh_field f);
  * stacked component; the layout conversion is a bit-exact permutation. */
 int mesh_field_import(mesh_field f, const void *host, size_t bytes);
 int mesh_field_export(mesh_field f, void *host, size_t bytes);
+/* Configuration files: the dataset writeToFile/readFromFile store
+ * ([nstack][sites lexicographic][reals], lattice.h:205-252) behind a 72-byte
+ * header (magic "MESHCFG1", version, group, precision, kind, nd, nstack,
+ * dims[4], trajectory, seed, checksum; little-endian). Loading refuses a file
+ * whose group, precision or grid differ from the field, as readConfig does
+ * (utils.h:188-219), with MESH_ERR_STATE; a corrupt file (checksum) also
+ * gives MESH_ERR_STATE. */
+int mesh_field_save(mesh_field f, const char *path);
+int mesh_field_load(mesh_field f, const char *path);
+/* header of a configuration file (any output may be NULL; dims gets nd values) */
+int mesh_config_info(const char *path, int *kind, int *group, int *precision, int *nd, int32_t *dims, int *nstack,
+                     uint64_t *trajectory, uint64_t *seed);
 /* deep copy (Lattice copy assignment, lattice.h:83-93); same shape required */
 int mesh_field_copy(mesh_field dst, mesh_field src);
 /* Lattice::zeros / fill_zeros (lattice.h:51-58) */
@@ -208,6 +220,12 @@ int mesh_hmc_field(mesh_hmc h, int which, mesh_field *out);
 /* randomizeGaugeField (hmc.cpp:397-400) and a cold start */
 int mesh_hmc_randomize(mesh_hmc h);
 int mesh_hmc_cold_start(mesh_hmc h);
+/* Checkpoint and resume: U, the trajectory counter and the seed in a
+ * configuration file. A chain with the same seed that loads it continues
+ * exactly as the saved chain would have (same momentum and Metropolis
+ * streams); records before the resume point read as zero. */
+int mesh_hmc_save(mesh_hmc h, const char *path);
+int mesh_hmc_load(mesh_hmc h, const char *path);
 /* runHmcUpdate (hmc.cpp:413-445): one trajectory, synchronous, record out */
 int mesh_hmc_update(mesh_hmc h, double beta, const double *deltas, int n, mesh_hmc_record *rec);
 /* One trajectory on caller-supplied momenta P0 (algebra field, copied, not
@@ -226,6 +244,38 @@ int mesh_hmc_history(mesh_hmc h, int first, int count, double *plaquette, double
  * call: import U from host, run `count` trajectories, export U to host. */
 int mesh_hmc_run_host(mesh_hmc h, void *host_U, size_t bytes, double beta, const double *deltas, int n, int count,
                       mesh_hmc_record *last);
+
+/* ---- batched replicas (no reference counterpart) --------------------------
+ * Many independent 4D lattices of one group and precision, each with its own
+ * extents, beta and seed, advanced together: every step of the trajectory
+ * sequence of runHmcUpdate (hmc.cpp:413-445) is one persistent launch over
+ * all replicas. Replica r follows the trajectory of a single chain
+ * (mesh_hmc_*) created with seeds[r]: same momentum and Metropolis streams,
+ * same per-link arithmetic. */
+typedef struct mesh_batch_s *mesh_batch;
+/* dims: nrep x 4 extents (even, < 256); seeds: nrep keys. Links start as unit. */
+int mesh_batch_create(mesh_ctx ctx, int group, int precision, int nrep, const int32_t *dims, const uint64_t *seeds,
+                      mesh_batch *out);
+int mesh_batch_destroy(mesh_batch h);
+int mesh_batch_size(mesh_batch h, int *nrep);
+/* Haar-random links (each replica as mesh_hmc_randomize with its seed) / unit links */
+int mesh_batch_randomize(mesh_batch h);
+int mesh_batch_cold_start(mesh_batch h);
+/* replica r's links in the reference's host layout (mesh_field_import/export) */
+int mesh_batch_import(mesh_batch h, int r, const void *host, size_t bytes);
+int mesh_batch_export(mesh_batch h, int r, void *host, size_t bytes);
+/* `count` trajectories of every replica, betas[r] per replica; use_graph != 0
+ * replays one captured trajectory of the whole batch. Synchronous. */
+int mesh_batch_run(mesh_batch h, const double *betas, const double *deltas, int n, int count, int use_graph);
+int mesh_batch_count(mesh_batch h, int *n);
+/* replica r's records [first, first+count) (any output may be NULL) */
+int mesh_batch_history(mesh_batch h, int r, int first, int count, double *plaquette, double *dH, double *accept);
+/* plaquette of every replica's current links (nrep values) */
+int mesh_batch_plaquettes(mesh_batch h, double *out);
+/* kernel launches per trajectory for an n_deltas-step table, and the
+ * persistent grids of the link and site kernels (any output may be NULL) */
+int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_deltas, int *grid_links,
+                           int *grid_sites);
 
 /* ---- Landau gauge fixing (src/gauge/landau.h) ----------------------------
  * g is a single-component group field (the gauge transform); U is not

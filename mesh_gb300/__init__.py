@@ -71,6 +71,12 @@ SIGNATURES = {
     "mesh_field_import": (_I, [_P, _P, _SZ]),
     "mesh_field_export": (_I, [_P, _P, _SZ]),
     "mesh_field_copy": (_I, [_P, _P]),
+    "mesh_field_save": (_I, [_P, C.c_char_p]),
+    "mesh_field_load": (_I, [_P, C.c_char_p]),
+    "mesh_config_info": (_I, [C.c_char_p, _IP, _IP, _IP, _IP, _I32P, _IP, C.POINTER(C.c_uint64),
+                              C.POINTER(C.c_uint64)]),
+    "mesh_hmc_save": (_I, [_P, C.c_char_p]),
+    "mesh_hmc_load": (_I, [_P, C.c_char_p]),
     "mesh_field_set_zero": (_I, [_P]),
     "mesh_field_set_unit": (_I, [_P]),
     "mesh_field_random": (_I, [_P, _U64, _U64]),
@@ -101,6 +107,18 @@ SIGNATURES = {
     "mesh_hmc_count": (_I, [_P, _IP]),
     "mesh_hmc_history": (_I, [_P, _I, _I, _DP, _DP, _DP]),
     "mesh_hmc_run_host": (_I, [_P, _P, _SZ, _D, _DP, _I, _I, C.POINTER(HmcRecord)]),
+    "mesh_batch_create": (_I, [_P, _I, _I, _I, _I32P, C.POINTER(C.c_uint64), _PP]),
+    "mesh_batch_destroy": (_I, [_P]),
+    "mesh_batch_size": (_I, [_P, _IP]),
+    "mesh_batch_randomize": (_I, [_P]),
+    "mesh_batch_cold_start": (_I, [_P]),
+    "mesh_batch_import": (_I, [_P, _I, _P, _SZ]),
+    "mesh_batch_export": (_I, [_P, _I, _P, _SZ]),
+    "mesh_batch_run": (_I, [_P, _DP, _DP, _I, _I, _I]),
+    "mesh_batch_count": (_I, [_P, _IP]),
+    "mesh_batch_history": (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
+    "mesh_batch_plaquettes": (_I, [_P, _DP]),
+    "mesh_batch_launch_info": (_I, [_P, _IP, _I, _IP, _IP]),
     "mesh_landau_functional": (_I, [_P, _P, _DP]),
     "mesh_landau_theta": (_I, [_P, _P, _DP]),
     "mesh_landau_deriv": (_I, [_P, _P, _P]),
@@ -271,6 +289,17 @@ class Field:
         _chk(load().mesh_field_copy(self.h, other.h))
         return self
 
+    def save(self, path: str):
+        """writeToFile (lattice.h:205-252): the host-layout dataset behind a
+        self-describing header"""
+        _chk(load().mesh_field_save(self.h, os.fsencode(path)))
+        return self
+
+    def load(self, path: str):
+        """readFromFile; refuses files of another group, precision or grid"""
+        _chk(load().mesh_field_load(self.h, os.fsencode(path)))
+        return self
+
     def set_zero(self):
         _chk(load().mesh_field_set_zero(self.h))
         return self
@@ -312,6 +341,28 @@ def GaugeField(ctx, group, prec, grid) -> Field:
 def Momenta(ctx, group, prec, grid) -> Field:
     """Conjugate momenta: nd algebra components."""
     return Field(ctx, ALGEBRA, group, prec, grid, grid.ndim)
+
+
+def config_info(path: str) -> dict:
+    """header of a configuration file"""
+    kind, group, prec, nd, nstack = (C.c_int() for _ in range(5))
+    dims = (C.c_int32 * 4)()
+    traj, seed = C.c_uint64(), C.c_uint64()
+    _chk(load().mesh_config_info(os.fsencode(path), C.byref(kind), C.byref(group), C.byref(prec), C.byref(nd), dims,
+                                 C.byref(nstack), C.byref(traj), C.byref(seed)))
+    return {"kind": kind.value, "group": group.value, "precision": prec.value, "dims": list(dims[:nd.value]),
+            "nstack": nstack.value, "trajectory": traj.value, "seed": seed.value}
+
+
+def read_config(ctx, path: str, expected_grid: "Grid | None" = None) -> Field:
+    """readConfig (utils.h:188-219): a new field with the file's grid and
+    group; refuses a file on another grid than `expected_grid`"""
+    info = config_info(path)
+    grid = Grid(info["dims"])
+    if expected_grid is not None and expected_grid != grid:
+        raise MeshError(3, f"grid mismatch on load. Expected {expected_grid.shape}, got {grid.shape}")
+    f = Field(ctx, info["kind"], info["group"], info["precision"], grid, info["nstack"])
+    return f.load(path)
 
 
 def Lattice(ctx, group, prec, grid, algebra: bool = False) -> Field:
@@ -457,6 +508,14 @@ class Hmc:
         a, p = _darr(deltas)
         _chk(load().mesh_hmc_run(self.h, beta, p, len(a), count, 1 if use_graph else 0))
 
+    def save(self, path: str):
+        """checkpoint: links, trajectory counter and seed"""
+        _chk(load().mesh_hmc_save(self.h, os.fsencode(path)))
+
+    def load(self, path: str):
+        """resume from a checkpoint written by a chain with the same seed"""
+        _chk(load().mesh_hmc_load(self.h, os.fsencode(path)))
+
     def run_host(self, host_U: np.ndarray, beta: float, deltas, count: int = 1) -> dict:
         a, p = _darr(deltas)
         rec = HmcRecord()
@@ -482,6 +541,85 @@ class Hmc:
     def close(self):
         if getattr(self, "h", None):
             load().mesh_hmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class HmcBatch:
+    """Independent 4D replicas (own extents, beta, seed) advanced together,
+    one persistent launch per trajectory step over all of them. Replica r
+    follows the trajectory of Hmc(ctx, group, prec, Grid(dims[r]), seeds[r])."""
+
+    def __init__(self, ctx: Context, group, prec: int, dims, seeds):
+        self.ctx, self.group, self.prec = ctx, group_code(group), prec
+        self.dims = [list(map(int, d)) for d in dims]
+        assert all(len(d) == 4 for d in self.dims), "replicas are 4D"
+        self.R = len(self.dims)
+        flat = (C.c_int32 * (4 * self.R))(*[x for d in self.dims for x in d])
+        sd = (C.c_uint64 * self.R)(*[int(x) for x in seeds])
+        h = C.c_void_p()
+        _chk(load().mesh_batch_create(ctx.h, self.group, prec, self.R, flat, sd, C.byref(h)))
+        self.h = h
+
+    def randomize_gauge_field(self):
+        _chk(load().mesh_batch_randomize(self.h))
+
+    def cold_start(self):
+        _chk(load().mesh_batch_cold_start(self.h))
+
+    def _host_shape(self, r):
+        return (4, int(np.prod(self.dims[r])), NREAL[self.group])
+
+    def export(self, r: int) -> np.ndarray:
+        out = np.zeros(self._host_shape(r), dtype=np.float32 if self.prec == F32 else np.float64)
+        _chk(load().mesh_batch_export(self.h, r, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def import_(self, r: int, host: np.ndarray):
+        a = np.ascontiguousarray(host, dtype=np.float32 if self.prec == F32 else np.float64)
+        assert a.shape == self._host_shape(r)
+        _chk(load().mesh_batch_import(self.h, r, a.ctypes.data_as(C.c_void_p), a.nbytes))
+        return self
+
+    def run(self, betas, deltas, count: int, use_graph: bool = True):
+        b, pb = _darr(betas)
+        if b.shape != (self.R,):
+            raise ValueError(f"expected {self.R} betas, one per replica")
+        a, p = _darr(deltas)
+        _chk(load().mesh_batch_run(self.h, pb, p, len(a), count, 1 if use_graph else 0))
+
+    @property
+    def count(self) -> int:
+        n = C.c_int()
+        _chk(load().mesh_batch_count(self.h, C.byref(n)))
+        return n.value
+
+    def history(self, r: int, first: int = 0, count: int | None = None):
+        if count is None:
+            count = self.count - first
+        pl, dh, ac = (np.zeros(count) for _ in range(3))
+        _chk(load().mesh_batch_history(self.h, r, first, count, pl.ctypes.data_as(_DP), dh.ctypes.data_as(_DP),
+                                       ac.ctypes.data_as(_DP)))
+        return {"plaq_history": pl, "deltaH_history": dh, "accept_history": ac}
+
+    def plaquettes(self) -> np.ndarray:
+        out = np.zeros(self.R)
+        _chk(load().mesh_batch_plaquettes(self.h, out.ctypes.data_as(_DP)))
+        return out
+
+    def launch_info(self, n_deltas: int):
+        lpt, gl, gs = C.c_int(), C.c_int(), C.c_int()
+        _chk(load().mesh_batch_launch_info(self.h, C.byref(lpt), n_deltas, C.byref(gl), C.byref(gs)))
+        return {"launches_per_trajectory": lpt.value, "grid_links": gl.value, "grid_sites": gs.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mesh_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

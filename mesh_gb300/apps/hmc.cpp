@@ -6,6 +6,8 @@
 //       -L mesh_gb300 -lmesh_gb300 -Wl,-rpath,$PWD/mesh_gb300 -o hmc
 //   ./hmc --group su3 --geom 8 8 8 8 --beta 5.7 --start cold --scheme 2lf
 //         --epsilon 0.5 --substeps 10 --count 20 --seed 1234 --precision 2
+//         [--checkpoint chain.bin]   links + trajectory counter at the end
+//         [--resume chain.bin]       continue a chain (same --seed) from a checkpoint
 #include "mesh/mesh.hpp"
 
 #include <chrono>
@@ -19,7 +21,7 @@ using namespace mesh;
 
 int main(int argc, char **argv)
 {
-	std::string group = "su3", scheme = "4mn", start = "random";
+	std::string group = "su3", scheme = "4mn", start = "random", resume, checkpoint;
 	std::vector<int32_t> geom = {8, 8, 8, 8};
 	double beta = 6.0, epsilon = 1.0;
 	int substeps = 8, count = 100, precision = 2;
@@ -59,6 +61,10 @@ int main(int argc, char **argv)
 			substeps = std::atoi(next());
 		else if (a == "--precision")
 			precision = std::atoi(next());
+		else if (a == "--resume")
+			resume = next();
+		else if (a == "--checkpoint")
+			checkpoint = next();
 		else
 		{
 			std::fprintf(stderr, "unknown option %s\n", a.c_str());
@@ -72,7 +78,9 @@ int main(int argc, char **argv)
 		    [&]<typename G>() {
 			    Grid g{Coordinate(geom.begin(), geom.end())};
 			    Hmc<G> hmc(g, seed);
-			    if (start == "random")
+			    if (!resume.empty())
+				    hmc.load(resume);
+			    else if (start == "random")
 				    hmc.randomizeGaugeField();
 			    else if (start == "cold")
 				    hmc.coldStart();
@@ -82,6 +90,8 @@ int main(int argc, char **argv)
 			    for (int iter = 0; iter < count; ++iter)
 				    hmc.runHmcUpdate(beta, deltas);
 			    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+			    if (!checkpoint.empty())
+				    hmc.save(checkpoint);
 			    hmc.print_summary();
 			    for (size_t k = 0; k < hmc.plaq_history.size(); ++k)
 				    std::printf("traj %zu plaq %.15f dH %.15e accept %.0f\n", k, hmc.plaq_history[k],

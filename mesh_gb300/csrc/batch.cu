@@ -1,0 +1,848 @@
+// Batched replicas: many independent 4D lattices of one group and precision,
+// each with its own extents, beta and seed, advanced together by the HMC
+// trajectory sequence of runHmcUpdate (src/gauge/hmc.cpp:413-445) in which
+// every step is ONE persistent launch over all replicas.
+//
+// Layout in HBM: one allocation per field kind (U, U_new, P) holding the
+// replicas' segments back to back (each 256-byte aligned), every segment in
+// the single-lattice layout (even/odd structure of arrays). A device table of
+// BatchRep descriptors holds each replica's geometry, pointers and seed.
+//
+// Work decomposition: the items of a launch (links: 4 planes of V_r per
+// replica, or sites: one plane of V_r) are cut into chunks of 256 items that
+// never straddle two planes or two replicas (a plane has ceil(V_r/256)
+// chunks), so a thread finds its direction and site without a division;
+// block b of the persistent grid takes the contiguous chunk range
+// [b cpb, (b+1) cpb). A block's replica therefore changes only at chunk
+// boundaries (a block-uniform event), which is where per-replica FP64 sums
+// are flushed: block sum -> partial [b][r] -> the last block adds, for each
+// replica, the partials of exactly the blocks that covered it, in block
+// order (deterministic for a given batch).
+//
+// Accept: the Metropolis kernel (one thread per replica) swaps the
+// replica's U and U_new pointers in the descriptor table instead of copying
+// the proposal, so an accepted trajectory costs no link traffic.
+//
+// Every per-link and per-site body is the single-lattice one (force_item,
+// the exp update, plaquette_site, the Philox momentum stream), so replica r
+// follows the same trajectory as a single chain with the same seed.
+#include "field.cuh"
+#include "kernels.cuh"
+#include "rng.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <vector>
+
+namespace meshgb {
+namespace {
+
+constexpr int kChunk = 256; // items per chunk = threads per block
+constexpr int kBND = 4;     // batches are 4D
+
+struct BatchRep
+{
+	Geom g;
+	void *U;       // accepted links
+	void *Unew;    // proposal (swapped with U on accept)
+	void *P;       // momenta
+	uint64_t seed; // Philox key of the replica's momentum and Metropolis streams
+	int64_t lchunk0, schunk0; // first chunk of the replica's links / sites
+	int32_t cpp;              // chunks per plane: ceil(V / 256)
+};
+
+// one item space (links or sites) of a batch and its persistent grid
+struct BatchSpace
+{
+	BatchRep const *reps;
+	int R;
+	bool sites;
+	int64_t nchunks; // total chunks over all replicas
+	int64_t cpb;     // chunks per block
+};
+
+struct BatchRed
+{
+	double *part;      // [gridDim][R]
+	double *result;    // [R]
+	unsigned *counter; // zero between launches
+};
+
+__device__ __forceinline__ int64_t chunk0_of(BatchSpace const &sp, int r)
+{
+	if (r >= sp.R)
+		return sp.nchunks;
+	return sp.sites ? sp.reps[r].schunk0 : sp.reps[r].lchunk0;
+}
+
+__device__ __forceinline__ int find_rep(BatchSpace const &sp, int64_t c)
+{
+	int lo = 0, hi = sp.R - 1;
+	while (lo < hi)
+	{
+		int mid = (lo + hi + 1) >> 1;
+		if (chunk0_of(sp, mid) <= c)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	return lo;
+}
+
+// sum over the block (valid in thread 0); every thread must call it
+__device__ __forceinline__ double block_sum(double v)
+{
+	__shared__ double sw[kChunk / 32];
+	v = warp_sum(v);
+	__syncthreads(); // sw may still be read by a previous call
+	if ((threadIdx.x & 31) == 0)
+		sw[threadIdx.x >> 5] = v;
+	__syncthreads();
+	double t = 0.0;
+	if (threadIdx.x == 0)
+		for (int i = 0; i < kChunk / 32; ++i)
+			t += sw[i];
+	return t;
+}
+
+// Runs body(r, rep, mu, s) -> double for the items of the block's chunk
+// range (mu: the direction plane, 0 for sites; s: the even/odd site); with
+// RED, per-replica sums of the returned values land in red.result[r]. The
+// replica's descriptor is reloaded only when the replica changes.
+template <bool RED, class Body> __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
+{
+	int64_t c0 = int64_t(blockIdx.x) * sp.cpb;
+	int64_t c1 = c0 + sp.cpb < sp.nchunks ? c0 + sp.cpb : sp.nchunks;
+	int r = c0 < c1 ? find_rep(sp, c0) : 0;
+	int64_t first = chunk0_of(sp, r), next = chunk0_of(sp, r + 1);
+	BatchRep rep = sp.reps[r];
+	int cur = r;
+	double acc = 0.0;
+	for (int64_t c = c0; c < c1; ++c)
+	{
+		if (c >= next)
+		{
+			if constexpr (RED)
+			{
+				double t = block_sum(acc);
+				if (threadIdx.x == 0)
+					red.part[int64_t(blockIdx.x) * sp.R + cur] = t;
+				acc = 0.0;
+			}
+			while (c >= next)
+			{
+				++r;
+				first = next;
+				next = chunk0_of(sp, r + 1);
+			}
+			rep = sp.reps[r];
+			cur = r;
+		}
+		uint32_t local = uint32_t(c - first);
+		uint32_t mu = local / uint32_t(rep.cpp);
+		int64_t s = int64_t(local - mu * uint32_t(rep.cpp)) * kChunk + threadIdx.x;
+		if (s < rep.g.V)
+			acc += body(r, rep, int(mu), s);
+	}
+	if constexpr (RED)
+	{
+		if (c0 < c1)
+		{
+			double t = block_sum(acc);
+			if (threadIdx.x == 0)
+				red.part[int64_t(blockIdx.x) * sp.R + cur] = t;
+		}
+		__shared__ bool is_last;
+		if (threadIdx.x == 0)
+		{
+			__threadfence();
+			unsigned prev = atomicInc(red.counter, gridDim.x - 1);
+			is_last = (prev == gridDim.x - 1);
+		}
+		__syncthreads();
+		if (is_last)
+		{
+			__threadfence();
+			for (int q = threadIdx.x; q < sp.R; q += blockDim.x)
+			{
+				int64_t blo = chunk0_of(sp, q) / sp.cpb, bhi = (chunk0_of(sp, q + 1) - 1) / sp.cpb;
+				double sum = 0.0;
+				for (int64_t b = blo; b <= bhi; ++b)
+					sum += __ldcg(red.part + b * sp.R + q);
+				red.result[q] = sum;
+			}
+		}
+	}
+}
+
+// Haar-random links (the stream of a single chain's randomize_gauge_field)
+template <int GRP, class T> __global__ void __launch_bounds__(kChunk) kb_random_links(BatchSpace sp)
+{
+	using Gp = Group<GRP, T>;
+	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s) {
+		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+		T p[Gp::NNORM_GROUP];
+		normals<T, Gp::NNORM_GROUP>(rep.seed, TAG_GAUGE, uint32_t(st.lex), uint32_t(mu), 0, p);
+		auto e = Gp::group_from_normals(p);
+		comp<T, Gp::NR>(static_cast<T *>(rep.U), rep.g.V, mu).store(s, e.v);
+		return 0.0;
+	});
+}
+
+template <int GRP, class T> __global__ void __launch_bounds__(kChunk) kb_unit_links(BatchSpace sp)
+{
+	using Gp = Group<GRP, T>;
+	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s) {
+		auto e = Gp::unit();
+		comp<T, Gp::NR>(static_cast<T *>(rep.U), rep.g.V, mu).store(s, e.v);
+		return 0.0;
+	});
+}
+
+// momentum refresh from the replica's stream at its trajectory counter, and
+// the kinetic energy
+template <int GRP, class T>
+__global__ void __launch_bounds__(kChunk) kb_refresh(BatchSpace sp, HmcDev const *__restrict__ dev, BatchRed kin)
+{
+	using Gp = Group<GRP, T>;
+	batch_loop<true>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s) {
+		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+		T p[Gp::DIM], o[Gp::NA];
+		normals<T, Gp::DIM>(rep.seed, TAG_MOMENTUM, uint32_t(st.lex), uint32_t(mu), dev[r].traj, p);
+		Gp::alg_from_normals(p, o);
+		comp<T, Gp::NA>(static_cast<T *>(rep.P), rep.g.V, mu).store(s, o);
+		return double(Gp::kin(o));
+	});
+}
+
+// U_new = exp(t P) (FIRST ? U : U_new), optionally reunitised
+template <int GRP, class T, bool FIRST, bool REUNIT>
+__global__ void __launch_bounds__(kChunk) kb_evolve(BatchSpace sp, T t)
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s) {
+		int64_t V = rep.g.V;
+		T p[Gp::NA];
+		comp<T, Gp::NA>(static_cast<T *>(rep.P), V, mu).load(s, p);
+		E u;
+		comp<T, Gp::NR>(static_cast<T *>(FIRST ? rep.U : rep.Unew), V, mu).load(s, u.v);
+		E x = Gp::mul(Gp::exp_alg(p, t), u);
+		if constexpr (REUNIT)
+			x = Gp::reunit_fast(x);
+		comp<T, Gp::NR>(static_cast<T *>(rep.Unew), V, mu).store(s, x.v);
+		return 0.0;
+	});
+}
+
+// P -= (beta_r / (2 Nc)) delta proj(U_new S); with KIN also the kinetic sums
+template <int GRP, class T, bool KIN>
+__global__ void __launch_bounds__(kChunk)
+    kb_force(BatchSpace sp, double const *__restrict__ beta, double delta, BatchRed kin)
+{
+	using Gp = Group<GRP, T>;
+	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s) {
+		int64_t V = rep.g.V;
+		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+		LinkLoad<GRP, T, kBND> ld{static_cast<T const *>(rep.Unew), V};
+		T coef = T(beta[r] / (2.0 * Gp::NC) * delta);
+		double k = force_item<GRP, T, kBND>(rep.g, st, s, mu, ld, static_cast<T *>(rep.P), coef);
+		return KIN ? k : 0.0;
+	});
+}
+
+// per-replica plaquette trace sums of U (NEW: of U_new)
+template <int GRP, class T, bool NEW> __global__ void __launch_bounds__(kChunk) kb_plaquette(BatchSpace sp, BatchRed out)
+{
+	batch_loop<true>(sp, out, [&](int, BatchRep const &rep, int, int64_t s) {
+		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+		LinkLoad<GRP, T, kBND> ld{static_cast<T const *>(NEW ? rep.Unew : rep.U), rep.g.V};
+		return double(plaquette_site<GRP, T, kBND>(rep.g, st, s, ld));
+	});
+}
+
+// Metropolis test per replica (k_metropolis for every replica); an accepted
+// proposal becomes the replica's links by a pointer swap
+__global__ void kb_metropolis(BatchRep *reps, int R, HmcDev *dev, HmcRecordDev *hist, int hist_cap,
+                              double const *beta, double *S_cur, double const *K_old, double const *S_new,
+                              double const *K_new, double Nc)
+{
+	int r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= R)
+		return;
+	double nplanes_V = 6.0 * double(reps[r].g.V);
+	double b = beta[r];
+	double plaq_old = S_cur[r] / nplanes_V / Nc;
+	double plaq_new = S_new[r] / nplanes_V / Nc;
+	double H_old = (1.0 - plaq_old) * (b * nplanes_V) + K_old[r];
+	double H_new = (1.0 - plaq_new) * (b * nplanes_V) + K_new[r];
+	double dH = H_new - H_old;
+	uint64_t traj = dev[r].traj;
+	double u = metropolis_uniform(reps[r].seed, traj);
+	bool finite = isfinite(H_old) && isfinite(H_new);
+	bool acc = finite && (u < exp(-dH));
+	if (!finite)
+		dev[r].bad = 1;
+	if (traj < uint64_t(hist_cap))
+	{
+		HmcRecordDev rec;
+		rec.plaq = acc ? plaq_new : plaq_old;
+		rec.dH = dH;
+		rec.accept = acc ? 1.0 : 0.0;
+		rec.H_old = H_old;
+		rec.H_new = H_new;
+		hist[int64_t(r) * hist_cap + int64_t(traj)] = rec;
+	}
+	if (acc)
+	{
+		S_cur[r] = S_new[r];
+		void *t = reps[r].U;
+		reps[r].U = reps[r].Unew;
+		reps[r].Unew = t;
+	}
+	dev[r].accept_last = acc ? 1 : 0;
+	dev[r].traj = traj + 1;
+}
+
+// launchers per (group, real type)
+struct BatchOps
+{
+	void (*random_links)(cudaStream_t, unsigned, BatchSpace);
+	void (*unit_links)(cudaStream_t, unsigned, BatchSpace);
+	void (*refresh)(cudaStream_t, unsigned, BatchSpace, HmcDev const *, BatchRed);
+	void (*evolve)(cudaStream_t, unsigned, BatchSpace, double, bool first, bool reunit);
+	void (*force)(cudaStream_t, unsigned, BatchSpace, double const *, double, BatchRed, bool kin);
+	void (*plaquette)(cudaStream_t, unsigned, BatchSpace, BatchRed, bool on_new);
+	int (*occupancy)(int which); // resident blocks per SM of kernel `which` (0 links-type, 1 force, 2 sites)
+};
+
+template <int GRP, class T> struct BatchImpl
+{
+	static void random_links(cudaStream_t st, unsigned g, BatchSpace sp)
+	{
+		kb_random_links<GRP, T><<<g, kChunk, 0, st>>>(sp);
+		MESH_LAUNCH_CHECK();
+	}
+	static void unit_links(cudaStream_t st, unsigned g, BatchSpace sp)
+	{
+		kb_unit_links<GRP, T><<<g, kChunk, 0, st>>>(sp);
+		MESH_LAUNCH_CHECK();
+	}
+	static void refresh(cudaStream_t st, unsigned g, BatchSpace sp, HmcDev const *dev, BatchRed kin)
+	{
+		kb_refresh<GRP, T><<<g, kChunk, 0, st>>>(sp, dev, kin);
+		MESH_LAUNCH_CHECK();
+	}
+	static void evolve(cudaStream_t st, unsigned g, BatchSpace sp, double t, bool first, bool reunit)
+	{
+		if (first && reunit)
+			kb_evolve<GRP, T, true, true><<<g, kChunk, 0, st>>>(sp, T(t));
+		else if (first)
+			kb_evolve<GRP, T, true, false><<<g, kChunk, 0, st>>>(sp, T(t));
+		else if (reunit)
+			kb_evolve<GRP, T, false, true><<<g, kChunk, 0, st>>>(sp, T(t));
+		else
+			kb_evolve<GRP, T, false, false><<<g, kChunk, 0, st>>>(sp, T(t));
+		MESH_LAUNCH_CHECK();
+	}
+	static void force(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double delta, BatchRed kin,
+	                  bool with_kin)
+	{
+		if (with_kin)
+			kb_force<GRP, T, true><<<g, kChunk, 0, st>>>(sp, beta, delta, kin);
+		else
+			kb_force<GRP, T, false><<<g, kChunk, 0, st>>>(sp, beta, delta, kin);
+		MESH_LAUNCH_CHECK();
+	}
+	static void plaquette(cudaStream_t st, unsigned g, BatchSpace sp, BatchRed out, bool on_new)
+	{
+		if (on_new)
+			kb_plaquette<GRP, T, true><<<g, kChunk, 0, st>>>(sp, out);
+		else
+			kb_plaquette<GRP, T, false><<<g, kChunk, 0, st>>>(sp, out);
+		MESH_LAUNCH_CHECK();
+	}
+	static int occupancy(int which)
+	{
+		int n = 0;
+		cudaError_t e;
+		if (which == 1)
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_force<GRP, T, true>, kChunk, 0);
+		else if (which == 2)
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_plaquette<GRP, T, true>, kChunk, 0);
+		else
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_evolve<GRP, T, false, true>, kChunk, 0);
+		MESH_CUDA(e);
+		return n;
+	}
+	static constexpr BatchOps ops{random_links, unit_links, refresh, evolve, force, plaquette, occupancy};
+};
+
+BatchOps const &batch_ops(int group, int prec)
+{
+	static BatchOps const t[3][2] = {{BatchImpl<U1, float>::ops, BatchImpl<U1, double>::ops},
+	                                 {BatchImpl<SU2, float>::ops, BatchImpl<SU2, double>::ops},
+	                                 {BatchImpl<SU3, float>::ops, BatchImpl<SU3, double>::ops}};
+	return t[group - 1][prec == MESH_F32 ? 0 : 1];
+}
+
+} // namespace
+} // namespace meshgb
+
+using namespace meshgb;
+
+struct mesh_batch_s
+{
+	Context *ctx = nullptr;
+	int group = 0, prec = 0, R = 0;
+	std::vector<int32_t> dims;  // R x 4
+	std::vector<BatchRep> reps; // host copy at creation (initial pointers)
+	void *bufU = nullptr, *bufUnew = nullptr, *bufP = nullptr;
+	BatchRep *d_reps = nullptr;
+	HmcDev *d_dev = nullptr;
+	HmcRecordDev *d_hist = nullptr;
+	int hist_cap = 0;
+	double *d_beta = nullptr;
+	double *d_part = nullptr, *d_res = nullptr; // partials [G][R]; results [4][R]
+	unsigned *d_cnt = nullptr;
+	BatchSpace links{}, sites{};
+	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
+	BatchSpace force_sp{};
+	int64_t count = 0;
+	bool S_valid = false;
+	cudaGraphExec_t graph = nullptr;
+	std::vector<double> graph_deltas;
+	HmcRecordDev *graph_hist = nullptr;
+
+	enum
+	{
+		S_CUR = 0,
+		K_OLD = 1,
+		S_NEW = 2,
+		K_NEW = 3,
+	};
+	BatchRed red(int k) { return {d_part, d_res + size_t(k) * R, d_cnt + k}; }
+	BatchOps const &ops() const { return batch_ops(group, prec); }
+
+	void drop_graph()
+	{
+		if (graph)
+			cudaGraphExecDestroy(graph);
+		graph = nullptr;
+	}
+
+	~mesh_batch_s()
+	{
+		if (!ctx)
+			return;
+		cudaSetDevice(ctx->device);
+		cudaStreamSynchronize(ctx->stream);
+		drop_graph();
+		for (void *p : {bufU, bufUnew, bufP, static_cast<void *>(d_reps), static_cast<void *>(d_dev),
+		                static_cast<void *>(d_hist), static_cast<void *>(d_beta), static_cast<void *>(d_part),
+		                static_cast<void *>(d_res), static_cast<void *>(d_cnt)})
+			if (p)
+				cudaFree(p);
+		ctx_release(ctx);
+	}
+
+	// space with its persistent grid: G = min(resident blocks, chunks)
+	static BatchSpace make_space(BatchRep const *reps, int R, bool sites, int64_t nchunks, int64_t target,
+	                             unsigned *grid)
+	{
+		int64_t G = std::max<int64_t>(1, std::min<int64_t>(target, nchunks));
+		int64_t cpb = (nchunks + G - 1) / G;
+		G = (nchunks + cpb - 1) / cpb;
+		*grid = unsigned(G);
+		return BatchSpace{reps, R, sites, nchunks, cpb};
+	}
+
+	void ensure_history(int64_t need)
+	{
+		if (need <= hist_cap)
+			return;
+		int cap = hist_cap ? hist_cap : 256;
+		while (cap < need)
+			cap *= 2;
+		HmcRecordDev *nh = nullptr;
+		MESH_CUDA(cudaMalloc(&nh, size_t(cap) * R * sizeof(HmcRecordDev)));
+		MESH_CUDA(cudaStreamSynchronize(ctx->stream));
+		if (d_hist)
+		{
+			MESH_CUDA(cudaMemcpy2D(nh, size_t(cap) * sizeof(HmcRecordDev), d_hist, size_t(hist_cap) * sizeof(HmcRecordDev),
+			                       size_t(hist_cap) * sizeof(HmcRecordDev), R, cudaMemcpyDeviceToDevice));
+			cudaFree(d_hist);
+		}
+		d_hist = nh;
+		hist_cap = cap;
+		drop_graph();
+	}
+
+	// one trajectory of every replica (runHmcUpdate, hmc.cpp:413-445)
+	void enqueue(double const *deltas, int n)
+	{
+		cudaStream_t st = ctx->stream;
+		auto const &o = ops();
+		if (!S_valid)
+		{
+			o.plaquette(st, g_sites, sites, red(S_CUR), false);
+			S_valid = true;
+		}
+		o.refresh(st, g_links, links, d_dev, red(K_OLD));
+		int last_p = n >= 3 ? n - 2 : -1;
+		for (int i = 0; i < n; ++i)
+		{
+			if (i % 2 == 0)
+				o.evolve(st, g_links, links, deltas[i], i == 0, i == n - 1);
+			else
+				o.force(st, g_force, force_sp, d_beta, deltas[i], red(K_NEW), i == last_p);
+		}
+		o.plaquette(st, g_sites, sites, red(S_NEW), true);
+		kb_metropolis<<<(R + 127) / 128, 128, 0, st>>>(d_reps, R, d_dev, d_hist, hist_cap, d_beta, d_res + size_t(S_CUR) * R,
+		                                             d_res + size_t(K_OLD) * R, d_res + size_t(S_NEW) * R,
+		                                             d_res + size_t(K_NEW) * R, double(group_nc(group)));
+		MESH_LAUNCH_CHECK();
+		++count;
+	}
+
+	// the replica's current link buffer (the descriptor table is updated on
+	// the device by accepted trajectories)
+	void *current_links(int r)
+	{
+		BatchRep rep;
+		MESH_CUDA(cudaMemcpyAsync(&rep, d_reps + r, sizeof(rep), cudaMemcpyDeviceToHost, ctx->stream));
+		MESH_CUDA(cudaStreamSynchronize(ctx->stream));
+		return rep.U;
+	}
+
+	Field view(int r, void *d)
+	{
+		Field f;
+		f.ctx = ctx;
+		f.kind = MESH_GROUP;
+		f.group = group;
+		f.prec = prec;
+		f.nd = kBND;
+		f.nstack = kBND;
+		for (int i = 0; i < kBND; ++i)
+			f.dims[i] = dims[size_t(r) * kBND + i];
+		f.geom = make_geom(kBND, f.dims);
+		f.nr = group_nr(group);
+		f.nr_host = group_nr(group);
+		f.real_bytes = prec == MESH_F32 ? 4 : 8;
+		f.bytes = size_t(kBND) * size_t(f.geom.V) * f.nr * f.real_bytes;
+		f.d = d;
+		return f;
+	}
+};
+
+namespace {
+int batch_api_fail(char const *msg)
+{
+	set_last_error(msg);
+	return MESH_ERR_ARG;
+}
+} // namespace
+
+extern "C" {
+
+int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t const *dims, uint64_t const *seeds,
+                      mesh_batch *out)
+{
+	if (!out)
+		return batch_api_fail("null output handle");
+	*out = nullptr;
+	if (!ctxh)
+		return batch_api_fail("null context");
+	auto *h = new mesh_batch_s();
+	int rc = api_call([&] {
+		require(group >= 1 && group <= 3, "unknown gauge group");
+		require(precision == MESH_F32 || precision == MESH_F64, "invalid precision level");
+		require(nrep >= 1 && nrep <= 4096, "number of replicas must be in [1, 4096]");
+		require(dims != nullptr && seeds != nullptr, "null dims or seeds");
+		Context &c = ctxh->c;
+		DeviceGuard dg(c.device);
+		h->group = group;
+		h->prec = precision;
+		h->R = nrep;
+		h->dims.assign(dims, dims + size_t(nrep) * kBND);
+		size_t rb = precision == MESH_F32 ? 4 : 8;
+		size_t nr = size_t(group_nr(group)), na = size_t(group_na(group));
+		auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
+		std::vector<size_t> offU(nrep), offP(nrep);
+		size_t totU = 0, totP = 0;
+		int64_t lch = 0, sch = 0;
+		h->reps.resize(nrep);
+		for (int r = 0; r < nrep; ++r)
+		{
+			int64_t V = 1;
+			for (int i = 0; i < kBND; ++i)
+			{
+				int32_t L = dims[size_t(r) * kBND + i];
+				require(L >= 2 && L % 2 == 0, "every extent must be even and >= 2 (checkerboard layout)");
+				require(L < 256, "every extent must be below 256");
+				V *= L;
+				require(V < (int64_t(1) << 31), "volume must be below 2^31");
+			}
+			BatchRep &rep = h->reps[r];
+			rep.g = make_geom(kBND, dims + size_t(r) * kBND);
+			rep.seed = seeds[r];
+			rep.lchunk0 = lch;
+			rep.schunk0 = sch;
+			rep.cpp = int32_t((V + kChunk - 1) / kChunk);
+			lch += int64_t(kBND) * rep.cpp;
+			sch += rep.cpp;
+			offU[r] = totU;
+			offP[r] = totP;
+			totU += align(size_t(kBND) * size_t(V) * nr * rb);
+			totP += align(size_t(kBND) * size_t(V) * na * rb);
+		}
+		MESH_CUDA(cudaMalloc(&h->bufU, totU));
+		MESH_CUDA(cudaMalloc(&h->bufUnew, totU));
+		MESH_CUDA(cudaMalloc(&h->bufP, totP));
+		for (int r = 0; r < nrep; ++r)
+		{
+			h->reps[r].U = static_cast<char *>(h->bufU) + offU[r];
+			h->reps[r].Unew = static_cast<char *>(h->bufUnew) + offU[r];
+			h->reps[r].P = static_cast<char *>(h->bufP) + offP[r];
+		}
+		MESH_CUDA(cudaMalloc(&h->d_reps, sizeof(BatchRep) * nrep));
+		MESH_CUDA(cudaMemcpy(h->d_reps, h->reps.data(), sizeof(BatchRep) * nrep, cudaMemcpyHostToDevice));
+		MESH_CUDA(cudaMalloc(&h->d_dev, sizeof(HmcDev) * nrep));
+		MESH_CUDA(cudaMemset(h->d_dev, 0, sizeof(HmcDev) * nrep));
+		MESH_CUDA(cudaMalloc(&h->d_beta, sizeof(double) * nrep));
+		MESH_CUDA(cudaMemset(h->d_beta, 0, sizeof(double) * nrep));
+		auto const &o = batch_ops(group, precision);
+		int64_t sms = c.num_sms;
+		h->links = mesh_batch_s::make_space(h->d_reps, nrep, false, lch, sms * std::min(8, o.occupancy(0)), &h->g_links);
+		h->force_sp =
+		    mesh_batch_s::make_space(h->d_reps, nrep, false, lch, sms * std::min(8, o.occupancy(1)), &h->g_force);
+		h->sites = mesh_batch_s::make_space(h->d_reps, nrep, true, sch, sms * std::min(8, o.occupancy(2)), &h->g_sites);
+		unsigned G = std::max({h->g_links, h->g_force, h->g_sites});
+		MESH_CUDA(cudaMalloc(&h->d_part, sizeof(double) * size_t(G) * nrep));
+		MESH_CUDA(cudaMalloc(&h->d_res, sizeof(double) * 4 * size_t(nrep)));
+		MESH_CUDA(cudaMemset(h->d_res, 0, sizeof(double) * 4 * size_t(nrep)));
+		MESH_CUDA(cudaMalloc(&h->d_cnt, sizeof(unsigned) * 4));
+		MESH_CUDA(cudaMemset(h->d_cnt, 0, sizeof(unsigned) * 4));
+		h->ctx = &c;
+		ctx_retain(c);
+		// unit links until the caller chooses a start
+		o.unit_links(c.stream, h->g_links, h->links);
+		MESH_CUDA(cudaStreamSynchronize(c.stream));
+	});
+	if (rc != MESH_OK)
+	{
+		if (!h->ctx)
+		{
+			for (void *p : {h->bufU, h->bufUnew, h->bufP, static_cast<void *>(h->d_reps), static_cast<void *>(h->d_dev),
+			                static_cast<void *>(h->d_beta), static_cast<void *>(h->d_part),
+			                static_cast<void *>(h->d_res), static_cast<void *>(h->d_cnt)})
+				if (p)
+					cudaFree(p);
+		}
+		delete h;
+		return rc;
+	}
+	*out = h;
+	return MESH_OK;
+}
+
+int mesh_batch_destroy(mesh_batch h)
+{
+	delete h;
+	return MESH_OK;
+}
+
+int mesh_batch_size(mesh_batch h, int *nrep)
+{
+	return api_call([&] {
+		require(h != nullptr && nrep != nullptr, "null argument");
+		*nrep = h->R;
+	});
+}
+
+int mesh_batch_randomize(mesh_batch h)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		DeviceGuard dg(h->ctx->device);
+		// descriptors back to the creation pointers, so that U is the buffer
+		// the random links go to whatever earlier trajectories swapped
+		MESH_CUDA(cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(BatchRep) * h->R, cudaMemcpyHostToDevice,
+		                          h->ctx->stream));
+		h->ops().random_links(h->ctx->stream, h->g_links, h->links);
+		h->S_valid = false;
+		MESH_CUDA(cudaStreamSynchronize(h->ctx->stream));
+	});
+}
+
+int mesh_batch_cold_start(mesh_batch h)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		DeviceGuard dg(h->ctx->device);
+		MESH_CUDA(cudaMemcpyAsync(h->d_reps, h->reps.data(), sizeof(BatchRep) * h->R, cudaMemcpyHostToDevice,
+		                          h->ctx->stream));
+		h->ops().unit_links(h->ctx->stream, h->g_links, h->links);
+		h->S_valid = false;
+		MESH_CUDA(cudaStreamSynchronize(h->ctx->stream));
+	});
+}
+
+int mesh_batch_import(mesh_batch h, int r, void const *host, size_t bytes)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		require(r >= 0 && r < h->R, "replica index out of range");
+		DeviceGuard dg(h->ctx->device);
+		Field f = h->view(r, h->current_links(r));
+		field_import_host(f, host, bytes);
+		h->S_valid = false;
+	});
+}
+
+int mesh_batch_export(mesh_batch h, int r, void *host, size_t bytes)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		require(r >= 0 && r < h->R, "replica index out of range");
+		DeviceGuard dg(h->ctx->device);
+		Field f = h->view(r, h->current_links(r));
+		field_export_host(f, host, bytes);
+	});
+}
+
+int mesh_batch_run(mesh_batch h, double const *betas, double const *deltas, int n, int count, int use_graph)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		require(betas != nullptr, "null betas");
+		require(deltas != nullptr && n >= 1, "empty step table");
+		require(n % 2 == 1, "step table must alternate position/momentum steps and have odd length");
+		require(count >= 0, "count must be >= 0");
+		for (int r = 0; r < h->R; ++r)
+			require(std::isfinite(betas[r]), "non-finite beta");
+		DeviceGuard dg(h->ctx->device);
+		cudaStream_t st = h->ctx->stream;
+		h->ensure_history(h->count + count);
+		// betas are read by the kernels from device memory: a captured
+		// trajectory stays valid when they change
+		MESH_CUDA(cudaMemcpyAsync(h->d_beta, betas, sizeof(double) * h->R, cudaMemcpyHostToDevice, st));
+		if (!use_graph)
+		{
+			for (int k = 0; k < count; ++k)
+				h->enqueue(deltas, n);
+			MESH_CUDA(cudaStreamSynchronize(st));
+			return;
+		}
+		if (!h->S_valid)
+		{
+			h->ops().plaquette(st, h->g_sites, h->sites, h->red(mesh_batch_s::S_CUR), false);
+			h->S_valid = true;
+		}
+		std::vector<double> dv(deltas, deltas + n);
+		if (!h->graph || h->graph_deltas != dv || h->graph_hist != h->d_hist)
+		{
+			h->drop_graph();
+			cudaGraph_t g = nullptr;
+			MESH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+			int64_t saved = h->count;
+			try
+			{
+				h->enqueue(deltas, n);
+			}
+			catch (...)
+			{
+				cudaStreamEndCapture(st, &g);
+				if (g)
+					cudaGraphDestroy(g);
+				throw;
+			}
+			h->count = saved;
+			MESH_CUDA(cudaStreamEndCapture(st, &g));
+			cudaGraphExec_t exec = nullptr;
+			cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+			cudaGraphDestroy(g);
+			MESH_CUDA(e);
+			h->graph = exec;
+			h->graph_deltas = dv;
+			h->graph_hist = h->d_hist;
+		}
+		for (int k = 0; k < count; ++k)
+			MESH_CUDA(cudaGraphLaunch(h->graph, st));
+		h->count += count;
+		MESH_CUDA(cudaStreamSynchronize(st));
+	});
+}
+
+int mesh_batch_count(mesh_batch h, int *n)
+{
+	return api_call([&] {
+		require(h != nullptr && n != nullptr, "null argument");
+		*n = int(h->count);
+	});
+}
+
+int mesh_batch_history(mesh_batch h, int r, int first, int count, double *plaquette, double *dH, double *accept)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		require(r >= 0 && r < h->R, "replica index out of range");
+		require(first >= 0 && count >= 0 && int64_t(first) + count <= h->count, "history range out of bounds");
+		DeviceGuard dg(h->ctx->device);
+		std::vector<HmcRecordDev> buf(static_cast<size_t>(count));
+		if (count)
+		{
+			MESH_CUDA(cudaMemcpyAsync(buf.data(), h->d_hist + int64_t(r) * h->hist_cap + first,
+			                          sizeof(HmcRecordDev) * size_t(count), cudaMemcpyDeviceToHost, h->ctx->stream));
+			MESH_CUDA(cudaStreamSynchronize(h->ctx->stream));
+		}
+		for (int k = 0; k < count; ++k)
+		{
+			if (plaquette)
+				plaquette[k] = buf[k].plaq;
+			if (dH)
+				dH[k] = buf[k].dH;
+			if (accept)
+				accept[k] = buf[k].accept;
+		}
+	});
+}
+
+int mesh_batch_plaquettes(mesh_batch h, double *out)
+{
+	return api_call([&] {
+		require(h != nullptr && out != nullptr, "null argument");
+		DeviceGuard dg(h->ctx->device);
+		cudaStream_t st = h->ctx->stream;
+		// S_CUR's slot is the trajectory's running action: use S_NEW's
+		h->ops().plaquette(st, h->g_sites, h->sites, h->red(mesh_batch_s::S_NEW), false);
+		std::vector<double> s(static_cast<size_t>(h->R));
+		MESH_CUDA(cudaMemcpyAsync(s.data(), h->d_res + size_t(mesh_batch_s::S_NEW) * h->R, sizeof(double) * h->R,
+		                          cudaMemcpyDeviceToHost, st));
+		MESH_CUDA(cudaStreamSynchronize(st));
+		for (int r = 0; r < h->R; ++r)
+		{
+			double V = double(h->reps[r].g.V);
+			out[r] = s[r] / (6.0 * V) / double(group_nc(h->group));
+		}
+	});
+}
+
+int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_deltas, int *grid_links, int *grid_sites)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		require(n_deltas >= 1 && n_deltas % 2 == 1, "step table length must be odd");
+		// refresh + n MD steps + plaquette + Metropolis
+		if (launches_per_trajectory)
+			*launches_per_trajectory = n_deltas + 3;
+		if (grid_links)
+			*grid_links = int(h->g_force);
+		if (grid_sites)
+			*grid_sites = int(h->g_sites);
+	});
+}
+
+} // extern "C"

@@ -198,6 +198,11 @@ void check_deltas(double const *deltas, int n)
 
 } // namespace
 
+void meshgb::ctx_retain(Context &c) { ++c.refs; }
+void meshgb::ctx_release(Context *c) { release_ctx(c); }
+void meshgb::field_import_host(Field &f, void const *host, size_t bytes) { import_host(f, host, bytes); }
+void meshgb::field_export_host(Field const &f, void *host, size_t bytes) { export_host(f, host, bytes); }
+
 // ---------------------------------------------------------------------------
 // HMC chain state
 // ---------------------------------------------------------------------------
@@ -443,6 +448,54 @@ int mesh_field_import(mesh_field h, void const *host, size_t bytes)
 int mesh_field_export(mesh_field h, void *host, size_t bytes)
 {
 	return api([&] { export_host(F(h), host, bytes); });
+}
+
+// ---- configuration files ---------------------------------------------------
+int mesh_field_save(mesh_field h, char const *path)
+{
+	return api([&] {
+		Field const &f = F(h);
+		std::vector<unsigned char> buf(f.host_bytes());
+		export_host(f, buf.data(), buf.size());
+		config_write(path, config_header_of(f, 0, 0), buf.data(), buf.size());
+	});
+}
+
+int mesh_field_load(mesh_field h, char const *path)
+{
+	return api([&] {
+		Field &f = F(h);
+		ConfigHeader hd = config_read_header(path);
+		config_check_matches(hd, f);
+		std::vector<unsigned char> buf(f.host_bytes());
+		config_read_data(path, hd, buf.data(), buf.size());
+		import_host(f, buf.data(), buf.size());
+	});
+}
+
+int mesh_config_info(char const *path, int *kind, int *group, int *precision, int *nd, int32_t *dims, int *nstack,
+                     uint64_t *trajectory, uint64_t *seed)
+{
+	return api([&] {
+		ConfigHeader hd = config_read_header(path);
+		if (kind)
+			*kind = hd.kind;
+		if (group)
+			*group = hd.group;
+		if (precision)
+			*precision = hd.precision;
+		if (nd)
+			*nd = hd.nd;
+		if (dims)
+			for (int i = 0; i < hd.nd; ++i)
+				dims[i] = hd.dims[i];
+		if (nstack)
+			*nstack = hd.nstack;
+		if (trajectory)
+			*trajectory = hd.trajectory;
+		if (seed)
+			*seed = hd.seed;
+	});
 }
 
 int mesh_field_copy(mesh_field dst, mesh_field src)
@@ -766,6 +819,46 @@ int mesh_hmc_cold_start(mesh_hmc h)
 		require(h != nullptr, "null hmc");
 		DeviceGuard dg(h->ctx->device);
 		ops_for(h->U.f).set_unit(h->U.f);
+		h->S_valid = false;
+	});
+}
+
+int mesh_hmc_save(mesh_hmc h, char const *path)
+{
+	return api([&] {
+		require(h != nullptr, "null hmc");
+		DeviceGuard dg(h->ctx->device);
+		uint64_t traj = 0;
+		MESH_CUDA(cudaMemcpyAsync(&traj, &h->d_dev->traj, sizeof(traj), cudaMemcpyDeviceToHost, h->ctx->stream));
+		Field const &u = h->U.f;
+		std::vector<unsigned char> buf(u.host_bytes());
+		export_host(u, buf.data(), buf.size()); // synchronises the stream
+		config_write(path, config_header_of(u, traj, h->seed), buf.data(), buf.size());
+	});
+}
+
+int mesh_hmc_load(mesh_hmc h, char const *path)
+{
+	return api([&] {
+		require(h != nullptr, "null hmc");
+		ConfigHeader hd = config_read_header(path);
+		Field &u = h->U.f;
+		config_check_matches(hd, u);
+		if (hd.seed != h->seed)
+			throw Error(MESH_ERR_STATE, "seed mismatch on resume (the chain's streams are keyed by its seed)");
+		require(hd.trajectory < uint64_t(1) << 30, "trajectory counter out of range");
+		std::vector<unsigned char> buf(u.host_bytes());
+		config_read_data(path, hd, buf.data(), buf.size());
+		DeviceGuard dg(h->ctx->device);
+		import_host(u, buf.data(), buf.size());
+		int64_t traj = int64_t(hd.trajectory);
+		h->ensure_history(traj + 1);
+		// records before the resume point are not in the file: zero them
+		MESH_CUDA(cudaMemsetAsync(h->d_hist, 0, sizeof(HmcRecordDev) * size_t(traj), h->ctx->stream));
+		uint64_t t = hd.trajectory;
+		MESH_CUDA(cudaMemcpyAsync(&h->d_dev->traj, &t, sizeof(t), cudaMemcpyHostToDevice, h->ctx->stream));
+		MESH_CUDA(cudaStreamSynchronize(h->ctx->stream));
+		h->count = traj;
 		h->S_valid = false;
 	});
 }

@@ -161,6 +161,32 @@ template <class F> int api_call(F &&f)
 	}
 }
 
+// context ownership and host <-> device layout conversion through the
+// context's staging buffer (capi.cu)
+void ctx_retain(Context &c);
+void ctx_release(Context *c);
+void field_import_host(Field &f, void const *host, size_t bytes);
+void field_export_host(Field const &f, void *host, size_t bytes);
+
+// configuration files (io.cu): header of the file format
+struct ConfigHeader
+{
+	char magic[8];
+	int32_t version;
+	int32_t group, precision, kind;
+	int32_t nd, nstack;
+	int32_t dims[4];
+	uint64_t trajectory;
+	uint64_t seed;
+	uint64_t checksum;
+};
+size_t config_data_bytes(ConfigHeader const &h);
+ConfigHeader config_header_of(Field const &f, uint64_t trajectory, uint64_t seed);
+void config_write(char const *path, ConfigHeader h, void const *data, size_t bytes);
+ConfigHeader config_read_header(char const *path);
+void config_read_data(char const *path, ConfigHeader const &h, void *data, size_t bytes);
+void config_check_matches(ConfigHeader const &h, Field const &f);
+
 // HMC trajectory kernels (hmc.cu)
 void launch_metropolis(Context &c, HmcDev *dev, HmcRecordDev *hist, double const *S_cur, double const *K_old,
                        double const *S_new, double const *K_new, double *S_cur_out, double beta, double nplanes_V,

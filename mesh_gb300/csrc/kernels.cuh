@@ -264,34 +264,42 @@ template <int GRP, class T, int ND> struct LinkLoad
 	}
 };
 
-// sum over sites and planes mu<nu of ReTr(U_mu(x) U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+)
+// sum over the planes mu<nu at site s of ReTr(U_mu(x) U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+)
 template <int GRP, class T, int ND>
-__global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restrict__ U, RedSlot out)
+__device__ __forceinline__ T plaquette_site(Geom const &g, Site<ND> const &st, int64_t s,
+                                            LinkLoad<GRP, T, ND> const &ld)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
+	T t = 0;
+#pragma unroll
+	for (int mu = 0; mu < ND; ++mu)
+	{
+		E a = ld(mu, s);
+		int64_t xm = eo_shift1<ND>(g, st, mu, +1);
+#pragma unroll
+		for (int nu = mu + 1; nu < ND; ++nu)
+		{
+			E b = ld(nu, xm);
+			E c = ld(mu, eo_shift1<ND>(g, st, nu, +1));
+			E d = ld(nu, s);
+			// ReTr((a b) (d c)^+)
+			t += Gp::retr_nd(Gp::mul(a, b), Gp::mul(d, c));
+		}
+	}
+	return t;
+}
+
+// sum over sites and planes of the plaquette traces
+template <int GRP, class T, int ND>
+__global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restrict__ U, RedSlot out)
+{
 	LinkLoad<GRP, T, ND> ld{U, g.V};
 	double acc = 0.0;
 	MESH_GRID_LOOP(s, g.V)
 	{
 		Site<ND> st = site_from_eo<ND>(g, s);
-		T t = 0;
-#pragma unroll
-		for (int mu = 0; mu < ND; ++mu)
-		{
-			E a = ld(mu, s);
-			int64_t xm = eo_shift1<ND>(g, st, mu, +1);
-#pragma unroll
-			for (int nu = mu + 1; nu < ND; ++nu)
-			{
-				E b = ld(nu, xm);
-				E c = ld(mu, eo_shift1<ND>(g, st, nu, +1));
-				E d = ld(nu, s);
-				// ReTr((a b) (d c)^+)
-				t += Gp::retr_nd(Gp::mul(a, b), Gp::mul(d, c));
-			}
-		}
-		acc += double(t);
+		acc += double(plaquette_site<GRP, T, ND>(g, st, s, ld));
 	}
 	grid_sum<kBlock>(acc, out);
 }

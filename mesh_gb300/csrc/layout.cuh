@@ -31,6 +31,11 @@ struct Geom
 	int L[4];
 	int64_t V, Vh;
 	int64_t stride[4]; // lexicographic stride of dimension i
+	// division by L[i] as a multiply and shift: n / L[i] == (n * dm[i]) >> ds[i]
+	// for every n < 2^31 (ds = 31 + ceil(log2 L), dm = floor(2^ds / L) + 1 <
+	// 2^33, so n * dm < 2^64; the rounding error n / 2^ds < 1 / L)
+	uint64_t dm[4];
+	int ds[4];
 
 	// extent / stride of a runtime direction through selects on constant
 	// offsets (indexing the kernel-parameter arrays with a runtime index
@@ -59,6 +64,14 @@ inline Geom make_geom(int nd, int32_t const *dims)
 	}
 	for (int i = nd; i < 4; ++i)
 		g.stride[i] = 0;
+	for (int i = 0; i < 4; ++i)
+	{
+		int l = 0;
+		while ((1 << l) < g.L[i])
+			++l;
+		g.ds[i] = 31 + l;
+		g.dm[i] = (uint64_t(1) << g.ds[i]) / uint64_t(g.L[i]) + 1;
+	}
 	g.Vh = g.V / 2;
 	return g;
 }
@@ -86,7 +99,7 @@ template <int ND> __device__ __forceinline__ Site<ND> site_from_eo(Geom const &g
 	for (int i = ND - 1; i >= 0; --i)
 	{
 		uint32_t L = uint32_t(g.L[i]);
-		uint32_t q = r / L;
+		uint32_t q = uint32_t((uint64_t(r) * g.dm[i]) >> g.ds[i]);
 		uint32_t xi = r - q * L;
 		px |= xi << (8 * i);
 		r = q;

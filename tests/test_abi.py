@@ -6,6 +6,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -70,3 +71,36 @@ def test_make_deltas_matches_oracle(oracle, libpath):
 
     for sch, eps, n in (("2lf", 0.5, 10), ("2mn", 0.5, 20), ("4mn", 1.0, 8), ("2lf", 0.5, 16)):
         np.testing.assert_array_equal(mg.make_deltas(sch, eps, n), oracle.make_deltas(sch, eps, n))
+
+
+def test_config_header_format_without_gpu(libpath, tmp_path):
+    """the configuration file header is read on the host: a file written
+    here by hand in the documented format is understood, a file with a wrong
+    magic is refused"""
+    import struct
+
+    import mesh_gb300 as mg
+
+    dims = [4, 6, 8, 2]
+    data = np.arange(4 * 4 * 6 * 8 * 2 * 4, dtype=np.float64)  # SU(2) FP64, 4 components
+    hdr = b"MESHCFG1" + struct.pack("<6i4iQQQ", 1, 2, 2, 0, 4, 4, *dims, 17, 99, 0)
+    assert len(hdr) == 72
+    path = tmp_path / "c.bin"
+    path.write_bytes(hdr + data.tobytes())
+    assert mg.config_info(str(path)) == {"kind": 0, "group": 2, "precision": 2, "dims": dims, "nstack": 4,
+                                         "trajectory": 17, "seed": 99}
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"NOTMESH!" + hdr[8:] + data.tobytes())
+    with pytest.raises(mg.MeshError):
+        mg.config_info(str(bad))
+
+
+def test_cpp_dropin_app_compiles(libpath, tmp_path):
+    """the converted src/apps/hmc.cpp builds on the C++ drop-in header and
+    links against the library (running it needs a GPU: test_gpu_app)"""
+    exe = tmp_path / "hmc"
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "mesh_gb300", "apps", "hmc.cpp"), "-L", os.path.dirname(libpath),
+                        "-lmesh_gb300", "-Wl,-rpath," + os.path.dirname(libpath), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
