@@ -459,9 +459,9 @@ def run_landau(args):
                 "fallbacks": int(sum(r["fallbacks"] for r in rows if r["method"] == m))}
             for m in ("or", "plain", "learned")}
     out = {"metric": "Landau gauge fixing seconds to theta<1e-12", "value": summ["learned"]["mean_seconds"],
-           "unit": "s", "n_gpus": 1, "steps": len(cfgs), "higher_is_better": False, "dtype": "f64",
+           "unit": "s", "n_gpus": 1, "steps": len(seeds), "higher_is_better": False, "dtype": "f64",
            "data": "synthetic", "config": {"workload": f"su3_landau_{L}^4_beta6.0_or1.7_vs_fa", "lattice": [L] * 4,
-                                           "thermalisation": f"{args.therm} trajectories, seeds 1..{len(cfgs)}",
+                                           "thermalisation": f"{args.therm} trajectories, seeds 1..{len(seeds)}",
                                            "transform": "Haar-random, seed 5"},
            "summary": summ, "speedup_learned_vs_or": summ["or"]["mean_seconds"] / summ["learned"]["mean_seconds"],
            "speedup_plain_fa_vs_or": summ["or"]["mean_seconds"] / summ["plain"]["mean_seconds"], "rows": rows}

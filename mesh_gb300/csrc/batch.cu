@@ -11,13 +11,13 @@
 // Work decomposition: the items of a launch (links: 4 planes of V_r per
 // replica, or sites: one plane of V_r) are cut into chunks of 256 items that
 // never straddle two planes or two replicas (a plane has ceil(V_r/256)
-// chunks), so a thread finds its direction and site without a division;
-// block b of the persistent grid takes the contiguous chunk range
-// [b cpb, (b+1) cpb). A block's replica therefore changes only at chunk
-// boundaries (a block-uniform event), which is where per-replica FP64 sums
-// are flushed: block sum -> partial [b][r] -> the last block adds, for each
-// replica, the partials of exactly the blocks that covered it, in block
-// order (deterministic for a given batch).
+// chunks), so a thread finds its direction and site without a division.
+// The persistent grid walks the chunks grid-stride, so all blocks sweep the
+// batch together and neighbouring links are shared in L2. A block's replica
+// changes only at chunk boundaries (a block-uniform event), which is where
+// per-replica FP64 sums are flushed: block sum -> partial [b][r] -> the last
+// block adds, for each replica, the partials of exactly the blocks that
+// covered it (deterministic for a given batch).
 //
 // Accept: the Metropolis kernel (one thread per replica) swaps the
 // replica's U and U_new pointers in the descriptor table instead of copying
@@ -59,7 +59,6 @@ struct BatchSpace
 	int R;
 	bool sites;
 	int64_t nchunks; // total chunks over all replicas
-	int64_t cpb;     // chunks per block
 };
 
 struct BatchRed
@@ -106,20 +105,27 @@ __device__ __forceinline__ double block_sum(double v)
 	return t;
 }
 
-// Runs body(r, rep, mu, s) -> double for the items of the block's chunk
-// range (mu: the direction plane, 0 for sites; s: the even/odd site); with
-// RED, per-replica sums of the returned values land in red.result[r]. The
-// replica's descriptor is reloaded only when the replica changes.
+// Runs body(r, rep, mu, s) -> double for the chunks c = blockIdx.x + k
+// gridDim.x (the whole grid sweeps the batch together, as a grid-stride loop
+// over one lattice does, so neighbouring links are shared in L2) with mu the
+// direction plane (0 for sites) and s the even/odd site. The replica only
+// grows along a block's chunks; the descriptor is reloaded when it changes.
+// With RED, a block's sum over one replica's chunks is flushed when the
+// replica changes (each (block, replica) pair once), and the last block adds
+// for replica q the partials of the blocks that covered q's chunks [a, b):
+// all blocks when b - a >= gridDim.x, else blocks a mod G .. (b-1) mod G, in
+// that order (deterministic for a given batch).
 template <bool RED, class Body> __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
 {
-	int64_t c0 = int64_t(blockIdx.x) * sp.cpb;
-	int64_t c1 = c0 + sp.cpb < sp.nchunks ? c0 + sp.cpb : sp.nchunks;
-	int r = c0 < c1 ? find_rep(sp, c0) : 0;
+	int64_t const G = gridDim.x;
+	int64_t c = blockIdx.x;
+	int r = c < sp.nchunks ? find_rep(sp, c) : 0;
 	int64_t first = chunk0_of(sp, r), next = chunk0_of(sp, r + 1);
 	BatchRep rep = sp.reps[r];
 	int cur = r;
+	bool touched = false;
 	double acc = 0.0;
-	for (int64_t c = c0; c < c1; ++c)
+	for (; c < sp.nchunks; c += G)
 	{
 		if (c >= next)
 		{
@@ -139,6 +145,7 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 			rep = sp.reps[r];
 			cur = r;
 		}
+		touched = true;
 		uint32_t local = uint32_t(c - first);
 		uint32_t mu = local / uint32_t(rep.cpp);
 		int64_t s = int64_t(local - mu * uint32_t(rep.cpp)) * kChunk + threadIdx.x;
@@ -147,7 +154,7 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 	}
 	if constexpr (RED)
 	{
-		if (c0 < c1)
+		if (touched)
 		{
 			double t = block_sum(acc);
 			if (threadIdx.x == 0)
@@ -166,10 +173,14 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 			__threadfence();
 			for (int q = threadIdx.x; q < sp.R; q += blockDim.x)
 			{
-				int64_t blo = chunk0_of(sp, q) / sp.cpb, bhi = (chunk0_of(sp, q + 1) - 1) / sp.cpb;
+				int64_t a = chunk0_of(sp, q), b = chunk0_of(sp, q + 1);
 				double sum = 0.0;
-				for (int64_t b = blo; b <= bhi; ++b)
-					sum += __ldcg(red.part + b * sp.R + q);
+				if (b - a >= G)
+					for (int64_t k = 0; k < G; ++k)
+						sum += __ldcg(red.part + k * sp.R + q);
+				else
+					for (int64_t k = a; k < b; ++k)
+						sum += __ldcg(red.part + (k % G) * sp.R + q);
 				red.result[q] = sum;
 			}
 		}
@@ -452,10 +463,8 @@ struct mesh_batch_s
 	                             unsigned *grid)
 	{
 		int64_t G = std::max<int64_t>(1, std::min<int64_t>(target, nchunks));
-		int64_t cpb = (nchunks + G - 1) / G;
-		G = (nchunks + cpb - 1) / cpb;
 		*grid = unsigned(G);
-		return BatchSpace{reps, R, sites, nchunks, cpb};
+		return BatchSpace{reps, R, sites, nchunks};
 	}
 
 	void ensure_history(int64_t need)

@@ -9,14 +9,15 @@ Method (no counterpart in the reference; written for this library):
   effective rate lambda depends on the configuration (beta) and on how far
   the fixing has got (theta).
 * Training data: on HMC-generated SU(3) configurations with random gauge
-  transforms, descent runs to theta < 1e-12; every few steps a trial line
-  search (mesh_landau_fa_trial, g unchanged) over a two-parameter multiplier
-  family m(p) = alpha p2max/p^2 max(1, boost 4 p2min/p^2) (step size and a
-  boost of the slow long-wavelength modes) picks the member that lowers theta
-  most. Its log multiplier at a set of momenta is the target for the
+  transforms, descent runs to theta < 1e-12; at the start of every decade of
+  theta a search over a two-parameter multiplier family
+  m(p) = alpha p2max/p^2 boost^w(p) (step size, and a factor on the
+  longest-wavelength modes fading out at 4 p2min) runs each member on a copy of g under
+  the solver's own fallback policy until theta has dropped tenfold and keeps
+  the cheapest (steps plus fallback sweeps). Its log multiplier at a set of momenta is the target for the
   features x = (log phat^2 - log p2max, 5 (beta - 6), (log10 theta + 7)/5).
-  The network amortises the line search: one inference per step instead of
-  a dozen trial steps. (mesh_landau_fa_probe, the per-momentum response, is
+  The network amortises the search: one inference per step instead of
+  twenty trial runs per decade. (mesh_landau_fa_probe, the per-momentum response, is
   kept as a diagnostic: a residual-weighted response is not a safe per-mode
   multiplier, as stiffer modes in a bin get over-stepped.)
 * Network: 3 -> 64 -> 64 -> 1 tanh MLP (FP32 weights), trained on the GPU by
@@ -53,11 +54,10 @@ def features(log_p2_rel, beta, theta):
 
 def hmc_configs(ctx, L, betas, seeds, therm, per_chain, spacing, eps=0.5, substeps=20):
     """SU(3) configurations from independent mixed-precision HMC chains (one
-    per (beta, seed)), returned as FP64 host arrays in the reference layout
-    together with their beta."""
+    per (beta, seed)), yielded one at a time as (beta, FP32 host array in the
+    reference layout); only the current chain is held."""
     grid = Grid([L] * 4)
     d = make_deltas("2mn", eps, substeps)
-    out = []
     for beta, seed in zip(betas, seeds):
         h = Hmc(ctx, 3, F32, grid, seed=int(seed))
         h.randomize_gauge_field()
@@ -65,9 +65,8 @@ def hmc_configs(ctx, L, betas, seeds, therm, per_chain, spacing, eps=0.5, subste
         for _ in range(per_chain):
             if spacing:
                 h.run(float(beta), d, spacing, use_graph=True)
-            out.append((float(beta), h.U.export().astype(np.float64)))
+            yield float(beta), h.U.export()
         h.close()
-    return out
 
 
 def prepared_links(ctx, U_host, transform_seed):
@@ -75,7 +74,7 @@ def prepared_links(ctx, U_host, transform_seed):
     and given a Haar-random gauge transform."""
     L = U_host.shape[1]
     dims = [int(round(L ** 0.25))] * 4
-    U = GaugeField(ctx, 3, F64, Grid(dims)).import_(U_host)
+    U = GaugeField(ctx, 3, F64, Grid(dims)).import_(U_host.astype(np.float64))
     reunitize(U)
     reunitize(U)
     h = Lattice(ctx, 3, F64, Grid(dims)).random(int(transform_seed))
@@ -83,60 +82,92 @@ def prepared_links(ctx, U_host, transform_seed):
     return U
 
 
-# multiplier family searched per step during data collection:
-#   m(p) = alpha * p2max/p^2 * max(1, boost * p2ref/p^2),  p2ref = 4 p2min
-ALPHAS = (0.03, 0.05, 0.08, 0.11)
-BOOSTS = (1.0, 2.0, 4.0)
+# multiplier family searched during data collection:
+#   m(p) = alpha p2max/p^2 * boost^w(p),  w = clip(log(p2ref/p^2) / log(p2ref/p2min), 0, 1),
+# p2ref = 4 p2min: boost scales the longest-wavelength modes (p^2 = p2min) and
+# fades out at p2ref; boost = 1 is the plain multiplier
+ALPHAS = (0.06, 0.08, 0.1, 0.12)
+BOOSTS = (0.5, 0.75, 1.0, 1.5)
 TABLE_N = 256
+
+
+def family_mult(alpha, boost, p2, p2min, p2max):
+    p2ref = 4.0 * p2min
+    w = np.clip(np.log(p2ref / p2) / np.log(p2ref / p2min), 0.0, 1.0)
+    return alpha * p2max / p2 * boost ** w
 
 
 def family_table(alpha, boost, p2min, p2max, n=TABLE_N):
     lo, hi = np.log(p2min) - 1e-3, np.log(p2max) + 1e-3
-    lp = np.linspace(lo, hi, n)
-    p2 = np.exp(lp)
-    m = alpha * p2max / p2 * np.maximum(1.0, boost * 4.0 * p2min / p2)
-    return np.log(m).astype(np.float32), lo, hi
+    p2 = np.exp(np.linspace(lo, hi, n))
+    return np.log(family_mult(alpha, boost, p2, p2min, p2max)).astype(np.float32), lo, hi
 
 
-def collect(ctx, U, beta, every=4, tol=1e-12, max_iter=1500, nbins=24):
-    """Samples along a data-collection run: every `every` steps a trial line
-    search over the multiplier family (alpha, boost) picks the member giving
-    the lowest theta after one step; its log multiplier at `nbins` momenta is
-    the target for features (log p^2/p2max, beta, theta). The run advances
-    with that member, overrelaxation sweeps when a step fails to lower theta.
-    Rows: (3 features, target)."""
+def collect(ctx, U, beta, tol=1e-12, nbins=24, max_steps=400, omega=1.7, or_sweeps=10, sample=None):
+    """Samples along a data-collection run, one set per decade of theta. At
+    the start of a decade every member (alpha, boost) of the multiplier
+    family runs on a copy of g under the solver's own policy (a step that
+    does not lower theta is undone and replaced by `or_sweeps`
+    overrelaxation sweeps) until theta has dropped tenfold; its cost is
+    steps + (or_sweeps + 1) x fallbacks (a step and a sweep cost about the
+    same). The cheapest member's log multiplier at `nbins` momenta is the
+    target for the features (log p^2/p2max, beta, theta) at the decade's
+    start and middle; g advances to that member's result. With `sample` (a
+    set of decade numbers, 0 = the first) only those decades are searched;
+    the others advance with the plain multiplier. Rows: (3 features,
+    target)."""
     fa = LandauFA(U)
     p2min, p2max = fa.p2range()
     g = Lattice(U.ctx, 3, F64, U.grid).set_unit()
+    trial = Lattice(U.ctx, 3, F64, U.grid)
+    best_g = Lattice(U.ctx, 3, F64, U.grid)
     rows = []
     centers = np.exp(np.linspace(np.log(p2min), np.log(p2max), nbins))
     lnd = Landau(U)
     lnd.g = g
-    it = 0
-    for it in range(max_iter):
+    cost_total = 0
+    collect.log = []
+    decade = -1
+    while True:
         th = fa.theta(g)
         if th < tol:
             break
-        if it % every == 0:
-            best = None
-            for a in ALPHAS:
-                for b in BOOSTS:
-                    fa.set_table(*family_table(a, b, p2min, p2max))
-                    after = fa.trial(g)[1]
-                    if best is None or after < best[0]:
-                        best = (after, a, b)
-            _, a, b = best
-            tab = family_table(a, b, p2min, p2max)
-            fa.set_table(*tab)
-            tgt = np.log(a * p2max / centers * np.maximum(1.0, b * 4.0 * p2min / centers))
-            rows.append(np.column_stack([features(np.log(centers) - np.log(p2max), beta, th), tgt]))
-        before, after = fa.trial(g)
-        if after < before:
-            fa.step(g)
-        else:
-            lnd.overrelax(1.7, tol=0.0, max_sweeps=10, check_every=10)
+        target = max(th / 10.0, tol)
+        decade += 1
+        if sample is not None and decade not in sample:
+            fa.set_plain(PLAIN_ALPHA)
+            it, fb, _ = fa.run(g, tol=target, max_iter=20 * max_steps, omega=omega, or_sweeps=or_sweeps)
+            cost_total += it + (or_sweeps + 1) * fb
+            continue
+        best = None
+        plain_cost = None
+        for a in ALPHAS:
+            for b in BOOSTS:
+                fa.set_table(*family_table(a, b, p2min, p2max))
+                trial.copy_from(g)
+                it, fb, th_end = fa.run(trial, tol=target, max_iter=max_steps, omega=omega, or_sweeps=or_sweeps)
+                if not th_end < target:
+                    continue
+                cost = it + (or_sweeps + 1) * fb
+                if a == PLAIN_ALPHA and b == 1.0:
+                    plain_cost = cost
+                if best is None or cost < best[0]:
+                    best = (cost, a, b)
+                    best_g.copy_from(trial)
+        collect.log.append({"theta": th, "plain_cost": plain_cost,
+                            "best": None if best is None else {"cost": best[0], "alpha": best[1], "boost": best[2]}})
+        if best is None:
+            it, _ = lnd.overrelax(omega, tol=target, max_sweeps=20 * max_steps, check_every=10)
+            cost_total += it
+            continue
+        cost, a, b = best
+        tgt = np.log(family_mult(a, b, centers, p2min, p2max))
+        for t in (th, th / np.sqrt(10.0)):
+            rows.append(np.column_stack([features(np.log(centers) - np.log(p2max), beta, t), tgt]))
+        g.copy_from(best_g)
+        cost_total += cost
     fa.close()
-    collect.last_iterations = it
+    collect.last_cost = cost_total
     return np.concatenate(rows) if rows else np.zeros((0, 4))
 
 
@@ -197,6 +228,8 @@ def main():
     ap.add_argument("--eval-therm", type=int, default=200)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--json", default=None)
+    ap.add_argument("--sample-decades", type=int, default=0,
+                    help="search this many random decades per configuration (0: every decade)")
     args = ap.parse_args()
     ctx = Context(0)
     if args.mode == "train":
@@ -206,22 +239,26 @@ def main():
         per_chain = max(1, args.configs // args.chains)
         cfgs = hmc_configs(ctx, args.L, betas, np.arange(1000, 1000 + args.chains), args.therm, per_chain,
                            args.spacing)
-        t_gen = time.time() - t0
         data = []
+        ncfg = 0
         for k, (beta, Uh) in enumerate(cfgs):
+            ncfg += 1
             U = prepared_links(ctx, Uh, transform_seed=5000 + k)
-            data.append(collect(ctx, U, beta))
-            print(json.dumps({"config": k, "beta": beta, "collect_iterations": collect.last_iterations,
+            sample = None
+            if args.sample_decades:
+                sample = set(int(x) for x in rng.choice(12, args.sample_decades, replace=False))
+            data.append(collect(ctx, U, beta, sample=sample))
+            print(json.dumps({"config": k, "beta": beta, "collect_cost": collect.last_cost, "decades": collect.log,
                               "rows": int(len(data[-1]))}), flush=True)
         data = np.concatenate(data)
-        t_collect = time.time() - t0 - t_gen
+        t_collect = time.time() - t0
         params, losses = train(ctx, data)
         np.savez(args.out, params=params, gamma=1.0, width=WIDTH, samples=len(data),
-                 final_loss=float(losses[-1]), first_loss=float(losses[0]), configs=len(cfgs), lattice=args.L,
+                 final_loss=float(losses[-1]), first_loss=float(losses[0]), configs=ncfg, lattice=args.L,
                  betas=betas)
         print(json.dumps({"samples": int(len(data)), "final_loss": float(losses[-1]),
                           "first_loss": float(losses[0]), "target_variance": float(np.var(data[:, 3])),
-                          "t_generate_s": t_gen, "t_collect_s": t_collect, "configs": len(cfgs)}))
+                          "t_generate_and_collect_s": t_collect, "configs": ncfg}))
     else:
         params, gamma = load_weights()
         seeds = np.arange(1, args.eval_configs + 1)
