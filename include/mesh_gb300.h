@@ -226,6 +226,10 @@ int mesh_hmc_cold_start(mesh_hmc h);
  * streams); records before the resume point read as zero. */
 int mesh_hmc_save(mesh_hmc h, const char *path);
 int mesh_hmc_load(mesh_hmc h, const char *path);
+/* One momentum step P -= beta/(2 Nc) delta proj(U S) on the chain's own U
+ * and P with the trajectory's kernel (SU(3) FP32 links read as rows 0 and 1,
+ * row 2 rebuilt; the autotuned launch variant): for timing and tests. */
+int mesh_hmc_momentum_step(mesh_hmc h, double beta, double delta);
 /* runHmcUpdate (hmc.cpp:413-445): one trajectory, synchronous, record out */
 int mesh_hmc_update(mesh_hmc h, double beta, const double *deltas, int n, mesh_hmc_record *rec);
 /* One trajectory on caller-supplied momenta P0 (algebra field, copied, not

@@ -76,6 +76,7 @@ SIGNATURES = {
     "mesh_config_info": (_I, [C.c_char_p, _IP, _IP, _IP, _IP, _I32P, _IP, C.POINTER(C.c_uint64),
                               C.POINTER(C.c_uint64)]),
     "mesh_hmc_save": (_I, [_P, C.c_char_p]),
+    "mesh_hmc_momentum_step": (_I, [_P, _D, _D]),
     "mesh_hmc_load": (_I, [_P, C.c_char_p]),
     "mesh_field_set_zero": (_I, [_P]),
     "mesh_field_set_unit": (_I, [_P]),
@@ -507,6 +508,10 @@ class Hmc:
     def run(self, beta: float, deltas, count: int, use_graph: bool = True):
         a, p = _darr(deltas)
         _chk(load().mesh_hmc_run(self.h, beta, p, len(a), count, 1 if use_graph else 0))
+
+    def momentum_step(self, beta: float, delta: float):
+        """the trajectory's momentum step on the chain's own U and P"""
+        _chk(load().mesh_hmc_momentum_step(self.h, beta, delta))
 
     def save(self, path: str):
         """checkpoint: links, trajectory counter and seed"""

@@ -23,9 +23,10 @@
 // replica's U and U_new pointers in the descriptor table instead of copying
 // the proposal, so an accepted trajectory costs no link traffic.
 //
-// Every per-link and per-site body is the single-lattice one (force_item,
-// the exp update, plaquette_site, the Philox momentum stream), so replica r
-// follows the same trajectory as a single chain with the same seed.
+// Every per-link and per-site body is the single-lattice trajectory's one
+// (force_item, the exp update, plaquette_site, the Philox momentum stream,
+// SU(3) FP32 links read as rows 0 and 1), so replica r follows the same
+// trajectory as a single chain with the same seed.
 #include "field.cuh"
 #include "kernels.cuh"
 #include "rng.cuh"
@@ -238,7 +239,14 @@ __global__ void __launch_bounds__(kChunk) kb_evolve(BatchSpace sp, T t)
 		T p[Gp::NA];
 		comp<T, Gp::NA>(static_cast<T *>(rep.P), V, mu).load(s, p);
 		E u;
-		comp<T, Gp::NR>(static_cast<T *>(FIRST ? rep.U : rep.Unew), V, mu).load(s, u.v);
+		T const *src = static_cast<T const *>(FIRST ? rep.U : rep.Unew);
+		if constexpr (kRows<GRP, T>)
+		{
+			Soa<T, Gp::NR>::template load_head<12>(src + int64_t(mu) * Gp::NR * V, V, s, u.v);
+			Gp::complete_row2(u);
+		}
+		else
+			comp<T, Gp::NR>(const_cast<T *>(src), V, mu).load(s, u.v);
 		E x = Gp::mul(Gp::exp_alg(p, t), u);
 		if constexpr (REUNIT)
 			x = Gp::reunit_fast(x);
@@ -256,7 +264,7 @@ __global__ void __launch_bounds__(kChunk)
 	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s) {
 		int64_t V = rep.g.V;
 		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
-		LinkLoad<GRP, T, kBND> ld{static_cast<T const *>(rep.Unew), V};
+		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(rep.Unew), V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * delta);
 		double k = force_item<GRP, T, kBND>(rep.g, st, s, mu, ld, static_cast<T *>(rep.P), coef);
 		return KIN ? k : 0.0;
@@ -268,7 +276,7 @@ template <int GRP, class T, bool NEW> __global__ void __launch_bounds__(kChunk) 
 {
 	batch_loop<true>(sp, out, [&](int, BatchRep const &rep, int, int64_t s) {
 		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
-		LinkLoad<GRP, T, kBND> ld{static_cast<T const *>(NEW ? rep.Unew : rep.U), rep.g.V};
+		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(NEW ? rep.Unew : rep.U), rep.g.V};
 		return double(plaquette_site<GRP, T, kBND>(rep.g, st, s, ld));
 	});
 }

@@ -274,7 +274,7 @@ struct mesh_hmc_s
 		Context &c = *ctx;
 		if (!S_valid)
 		{
-			ops.plaquette(u, rs(S_CUR));
+			ops.hmc_plaquette(u, rs(S_CUR));
 			S_valid = true;
 		}
 		if (P0)
@@ -289,16 +289,16 @@ struct mesh_hmc_s
 		for (int i = 0; i < n; ++i)
 		{
 			if (i % 2 == 0)
-				ops.evolve(i == 0 ? u : un, un, p, deltas[i], i == n - 1);
+				ops.hmc_evolve(i == 0 ? u : un, un, p, deltas[i], i == n - 1);
 			else
 			{
 				RedSlot kin = rs(K_NEW);
-				ops.momentum_step(p, un, coef0 * deltas[i], i == last_p ? &kin : nullptr);
+				ops.hmc_momentum_step(p, un, coef0 * deltas[i], i == last_p ? &kin : nullptr);
 			}
 		}
 		if (last_p < 0)
 			ops.norm2(p, rs(K_NEW));
-		ops.plaquette(un, rs(S_NEW));
+		ops.hmc_plaquette(un, rs(S_NEW));
 		double *res = d_res;
 		launch_metropolis(c, d_dev, d_hist, res + S_CUR, res + K_OLD, res + S_NEW, res + K_NEW, res + S_CUR, beta,
 		                  nplanes(u.nd) * double(u.geom.V), double(group_nc(u.group)), seed, uniform, d_flag);
@@ -863,6 +863,16 @@ int mesh_hmc_load(mesh_hmc h, char const *path)
 	});
 }
 
+int mesh_hmc_momentum_step(mesh_hmc h, double beta, double delta)
+{
+	return api([&] {
+		require(h != nullptr, "null hmc");
+		DeviceGuard dg(h->ctx->device);
+		Field &U = h->U.f, &P = h->P.f;
+		ops_for(U).hmc_momentum_step(P, U, beta / (2.0 * group_nc(U.group)) * delta, nullptr);
+	});
+}
+
 static void copy_rec(HmcRecordDev const &r, mesh_hmc_record *rec)
 {
 	if (!rec)
@@ -925,11 +935,11 @@ int mesh_hmc_run(mesh_hmc h, double beta, double const *deltas, int n, int count
 		}
 		if (!h->S_valid)
 		{
-			ops_for(h->U.f).plaquette(h->U.f, h->rs(mesh_hmc_s::S_CUR));
+			ops_for(h->U.f).hmc_plaquette(h->U.f, h->rs(mesh_hmc_s::S_CUR));
 			h->S_valid = true;
 		}
 		// choose launch variants before capturing (tuning times kernels)
-		ops_for(h->U.f).tune(h->P.f, h->Unew.f);
+		ops_for(h->U.f).hmc_tune(h->P.f, h->Unew.f);
 		std::vector<double> dv(deltas, deltas + n);
 		if (!h->graph || h->graph_beta != beta || h->graph_deltas != dv || h->graph_hist != h->d_hist)
 		{

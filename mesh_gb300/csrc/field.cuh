@@ -106,6 +106,13 @@ struct OpsTable
 	void (*gauge_transform)(Field &U, Field const &g);
 	// pick launch variants for U's lattice ahead of a stream capture
 	void (*tune)(Field &P, Field const &U);
+	// the HMC trajectory's plaquette, link update, momentum step and tuning:
+	// links known to be special unitary (SU(3) FP32 links are read as rows 0
+	// and 1, row 2 rebuilt); the same as the generic ones otherwise
+	void (*hmc_plaquette)(Field const &U, RedSlot out);
+	void (*hmc_evolve)(Field const &Usrc, Field &Udst, Field const &P, double t, bool reunit);
+	void (*hmc_momentum_step)(Field &P, Field const &U, double coef, RedSlot *kin);
+	void (*hmc_tune)(Field &P, Field const &U);
 };
 
 // autotuning registry (tune.cu): variant index per kernel/lattice key

@@ -492,6 +492,13 @@ template <class T> struct Group<SU3, T>
 				o.set(i, j, cmul(r.at(i, j), f));
 		return o;
 	}
+	// row 2 of a special unitary matrix from rows 0 and 1: conj(row0 x row1)
+	MESH_HD static void complete_row2(E &r)
+	{
+		r.set(2, 0, cconj(csub(cmul(r.at(0, 1), r.at(1, 2)), cmul(r.at(0, 2), r.at(1, 1)))));
+		r.set(2, 1, cconj(csub(cmul(r.at(0, 2), r.at(1, 0)), cmul(r.at(0, 0), r.at(1, 2)))));
+		r.set(2, 2, cconj(csub(cmul(r.at(0, 0), r.at(1, 1)), cmul(r.at(0, 1), r.at(1, 0)))));
+	}
 	// exact: Gram-Schmidt rows 0,1; row 2 = conj(row0 x row1)
 	MESH_HD static E reunit_exact(E const &a)
 	{

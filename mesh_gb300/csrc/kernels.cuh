@@ -250,7 +250,12 @@ __global__ void __launch_bounds__(kBlock) k_sum_real_trace(int64_t V, T const *_
 // ---------------------------------------------------------------------------
 // gauge action and force
 // ---------------------------------------------------------------------------
-template <int GRP, class T, int ND> struct LinkLoad
+// Link loads of a gauge field. ROWS: SU(3) links are read as their rows 0
+// and 1 (the first 12 reals: whole leading planes of the layout) and row 2
+// is rebuilt as conj(row0 x row1), which is exact for special unitary
+// matrices: a third less link traffic. Used only where the links are SU(3)
+// by construction (the HMC trajectory and the batched replicas).
+template <int GRP, class T, int ND, bool ROWS = false> struct LinkLoad
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
@@ -259,15 +264,23 @@ template <int GRP, class T, int ND> struct LinkLoad
 	__device__ __forceinline__ E operator()(int mu, int64_t s) const
 	{
 		E e;
-		Soa<T, Gp::NR>::template load<CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
+		if constexpr (ROWS && GRP == SU3)
+		{
+			Soa<T, Gp::NR>::template load_head<12, CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
+			Gp::complete_row2(e);
+		}
+		else
+			Soa<T, Gp::NR>::template load<CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
 		return e;
 	}
 };
 
+// rebuilt-row link loads for SU(3) in FP32 (the mixed-precision HMC links)
+template <int GRP, class T> inline constexpr bool kRows = GRP == SU3 && sizeof(T) == 4;
+
 // sum over the planes mu<nu at site s of ReTr(U_mu(x) U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+)
-template <int GRP, class T, int ND>
-__device__ __forceinline__ T plaquette_site(Geom const &g, Site<ND> const &st, int64_t s,
-                                            LinkLoad<GRP, T, ND> const &ld)
+template <int GRP, class T, int ND, class LD>
+__device__ __forceinline__ T plaquette_site(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
@@ -291,10 +304,10 @@ __device__ __forceinline__ T plaquette_site(Geom const &g, Site<ND> const &st, i
 }
 
 // sum over sites and planes of the plaquette traces
-template <int GRP, class T, int ND>
+template <int GRP, class T, int ND, bool ROWS = false>
 __global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restrict__ U, RedSlot out)
 {
-	LinkLoad<GRP, T, ND> ld{U, g.V};
+	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
 	double acc = 0.0;
 	MESH_GRID_LOOP(s, g.V)
 	{
@@ -326,9 +339,9 @@ template <> struct Prod<SU3, float, true>
 // U_nu(x+mu) (U_nu(x) U_mu(x+nu))^+ then the lower staple
 // (U_mu(y) U_nu(y+mu))^+ U_nu(y) at y = x - nu. Runtime mu and a rolled nu
 // loop keep one copy of the SU(3) body in the instruction cache.
-template <int GRP, class T, int ND, bool F2 = false>
+template <int GRP, class T, int ND, bool F2 = false, class LD>
 __device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<ND> const &st, int64_t s, int mu,
-                                                            LinkLoad<GRP, T, ND> const &ld)
+                                                            LD const &ld)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
@@ -359,9 +372,9 @@ __device__ __forceinline__ typename Group<GRP, T>::E staple(Geom const &g, Site<
 
 // one link's momentum update: P_mu(x) -= coef proj(U_mu(x) S_mu(x)); returns
 // the kinetic norm of the updated momentum
-template <int GRP, class T, int ND, bool F2 = false>
-__device__ __forceinline__ double force_item(Geom const &g, Site<ND> const &st, int64_t s, int mu,
-                                             LinkLoad<GRP, T, ND> const &ld, T *__restrict__ P, T coef)
+template <int GRP, class T, int ND, bool F2 = false, class LD>
+__device__ __forceinline__ double force_item(Geom const &g, Site<ND> const &st, int64_t s, int mu, LD const &ld,
+                                             T *__restrict__ P, T coef)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
@@ -379,11 +392,11 @@ __device__ __forceinline__ double force_item(Geom const &g, Site<ND> const &st, 
 }
 
 // Momentum step, one thread per (site, mu) in even/odd order.
-template <int GRP, class T, int ND, int NT, int MINB>
+template <int GRP, class T, int ND, int NT, int MINB, bool ROWS = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step(Geom g, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin)
 {
-	LinkLoad<GRP, T, ND> ld{U, g.V};
+	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
 	double acc = 0.0;
 	int64_t n = int64_t(ND) * g.V;
 	for (int64_t i = int64_t(blockIdx.x) * NT + threadIdx.x; i < n; i += int64_t(gridDim.x) * NT)
@@ -408,11 +421,11 @@ struct TileSpec
 	int ntiles; // tiles in the lattice
 };
 
-template <int GRP, class T, int ND, int NT, int MINB, bool F2 = false>
+template <int GRP, class T, int ND, int NT, int MINB, bool F2 = false, bool ROWS = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_tiled(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin)
 {
-	LinkLoad<GRP, T, ND> ld{U, g.V};
+	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
 	double acc = 0.0;
 	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
 	{
@@ -481,7 +494,7 @@ __global__ void __launch_bounds__(kBlock)
 }
 
 // U_dst = exp(t P) U_src for every (site, mu); optional project_on_group_fast
-template <int GRP, class T, bool REUNIT>
+template <int GRP, class T, bool REUNIT, bool ROWS = false>
 __global__ void __launch_bounds__(kBlock)
     k_evolve(int64_t n_total, int64_t V, T const *__restrict__ Usrc, T *__restrict__ Udst, T const *__restrict__ P,
              T t)
@@ -495,7 +508,13 @@ __global__ void __launch_bounds__(kBlock)
 		T p[Gp::NA];
 		comp<T, Gp::NA>(const_cast<T *>(P), V, mu).load(s, p);
 		E u;
-		comp<T, Gp::NR>(const_cast<T *>(Usrc), V, mu).load(s, u.v);
+		if constexpr (ROWS && GRP == SU3)
+		{
+			Soa<T, Gp::NR>::template load_head<12>(Usrc + int64_t(mu) * Gp::NR * V, V, s, u.v);
+			Gp::complete_row2(u);
+		}
+		else
+			comp<T, Gp::NR>(const_cast<T *>(Usrc), V, mu).load(s, u.v);
 		E r = Gp::mul(Gp::exp_alg(p, t), u);
 		if constexpr (REUNIT)
 			r = Gp::reunit_fast(r);
@@ -950,6 +969,19 @@ template <int GRP, class T, int ND> struct Ops
 		    U.geom, static_cast<T const *>(U.d), out);
 		MESH_LAUNCH_CHECK();
 	}
+	// the HMC trajectory's versions: SU(3) FP32 links read as rows 0, 1
+	static void hmc_plaquette(Field const &U, RedSlot out)
+	{
+		if constexpr (kRows<GRP, T>)
+		{
+			auto &c = *U.ctx;
+			k_plaquette<GRP, T, ND, true><<<red_blocks(c, U.geom.V), kBlock, 0, c.stream>>>(
+			    U.geom, static_cast<T const *>(U.d), out);
+			MESH_LAUNCH_CHECK();
+		}
+		else
+			plaquette(U, out);
+	}
 	static void staple_sum(Field &S, Field const &U, int mu)
 	{
 		auto &c = *U.ctx;
@@ -977,6 +1009,25 @@ template <int GRP, class T, int ND> struct Ops
 		int64_t n = int64_t(U.nstack) * U.geom.V;
 		k_reunit<GRP, T, true><<<blocks(c, n), kBlock, 0, c.stream>>>(n, U.geom.V, static_cast<T *>(U.d));
 		MESH_LAUNCH_CHECK();
+	}
+	static void hmc_evolve(Field const &Usrc, Field &Udst, Field const &P, double t, bool reunit)
+	{
+		if constexpr (kRows<GRP, T>)
+		{
+			auto &c = *Udst.ctx;
+			int64_t n = int64_t(Udst.nstack) * Udst.geom.V;
+			if (reunit)
+				k_evolve<GRP, T, true, true><<<blocks(c, n), kBlock, 0, c.stream>>>(
+				    n, Udst.geom.V, static_cast<T const *>(Usrc.d), static_cast<T *>(Udst.d),
+				    static_cast<T const *>(P.d), T(t));
+			else
+				k_evolve<GRP, T, false, true><<<blocks(c, n), kBlock, 0, c.stream>>>(
+				    n, Udst.geom.V, static_cast<T const *>(Usrc.d), static_cast<T *>(Udst.d),
+				    static_cast<T const *>(P.d), T(t));
+			MESH_LAUNCH_CHECK();
+		}
+		else
+			evolve(Usrc, Udst, P, t, reunit);
 	}
 	static void evolve(Field const &Usrc, Field &Udst, Field const &P, double t, bool reunit)
 	{
@@ -1033,7 +1084,14 @@ template <int GRP, class T, int ND> struct Ops
 				return false;
 		return true;
 	}
-	static void launch_force(int v, Field &P, Field const &U, T coef, RedSlot kin)
+	static void launch_force(int v, Field &P, Field const &U, T coef, RedSlot kin, bool rows = false)
+	{
+		if constexpr (kRows<GRP, T>)
+			if (rows)
+				return launch_force_t<true>(v, P, U, coef, kin);
+		launch_force_t<false>(v, P, U, coef, kin);
+	}
+	template <bool ROWS> static void launch_force_t(int v, Field &P, Field const &U, T coef, RedSlot kin)
 	{
 		auto &c = *U.ctx;
 		Geom const &g = U.geom;
@@ -1047,9 +1105,9 @@ template <int GRP, class T, int ND> struct Ops
 			if (b > unsigned(kMaxRedBlocks))
 				b = kMaxRedBlocks;
 			if (fv.minb == 1)
-				k_momentum_step<GRP, T, ND, 256, 1><<<b, 256, 0, c.stream>>>(g, u, p, coef, kin);
+				k_momentum_step<GRP, T, ND, 256, 1, ROWS><<<b, 256, 0, c.stream>>>(g, u, p, coef, kin);
 			else
-				k_momentum_step<GRP, T, ND, 256, 2><<<b, 256, 0, c.stream>>>(g, u, p, coef, kin);
+				k_momentum_step<GRP, T, ND, 256, 2, ROWS><<<b, 256, 0, c.stream>>>(g, u, p, coef, kin);
 		}
 		else if constexpr (ND == 4)
 		{
@@ -1070,39 +1128,44 @@ template <int GRP, class T, int ND> struct Ops
 				if constexpr (kF2)
 				{
 					if (fv.threads == 128 && fv.minb == 4)
-						k_momentum_step_tiled<GRP, T, 4, 128, 4, true><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+						k_momentum_step_tiled<GRP, T, 4, 128, 4, true, ROWS>
+						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
 					else if (fv.threads == 128)
-						k_momentum_step_tiled<GRP, T, 4, 128, 3, true><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+						k_momentum_step_tiled<GRP, T, 4, 128, 3, true, ROWS>
+						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
 					else
-						k_momentum_step_tiled<GRP, T, 4, 256, 2, true><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+						k_momentum_step_tiled<GRP, T, 4, 256, 2, true, ROWS>
+						    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
 				}
 			}
 			else if (fv.threads == 256 && fv.minb == 1)
-				k_momentum_step_tiled<GRP, T, 4, 256, 1><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				k_momentum_step_tiled<GRP, T, 4, 256, 1, false, ROWS><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
 			else if (fv.threads == 256 && fv.minb == 2)
-				k_momentum_step_tiled<GRP, T, 4, 256, 2><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				k_momentum_step_tiled<GRP, T, 4, 256, 2, false, ROWS><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
 			else if (fv.threads == 128 && fv.minb == 3)
-				k_momentum_step_tiled<GRP, T, 4, 128, 3><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				k_momentum_step_tiled<GRP, T, 4, 128, 3, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
 			else
-				k_momentum_step_tiled<GRP, T, 4, 128, 4><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				k_momentum_step_tiled<GRP, T, 4, 128, 4, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
 		}
 		MESH_LAUNCH_CHECK();
 	}
-	static std::string force_key(Field const &U)
+	static std::string force_key(Field const &U, bool rows)
 	{
 		std::string k = "momentum_step/group" + std::to_string(GRP) + "/" + (sizeof(T) == 4 ? "f32" : "f64") + "/";
 		for (int i = 0; i < ND; ++i)
 			k += (i ? "x" : "") + std::to_string(U.dims[i]);
+		if (rows && kRows<GRP, T>)
+			k += "/rows01";
 		return k;
 	}
 	// fastest valid variant for this lattice, timed once with coef = 0 (the
 	// momenta are rewritten unchanged); not while the stream is capturing
-	static int choose_force(Field &P, Field const &U)
+	static int choose_force(Field &P, Field const &U, bool rows = false)
 	{
 		int ov = force_override();
 		if (ov >= 0 && ov < n_force_variants() && force_variant_valid(U.geom, ov))
 			return ov;
-		std::string key = force_key(U);
+		std::string key = force_key(U, rows);
 		int v = tuned_variant(key);
 		if (v >= 0)
 			return v;
@@ -1122,10 +1185,10 @@ template <int GRP, class T, int ND> struct Ops
 		{
 			if (!force_variant_valid(U.geom, cand))
 				continue;
-			launch_force(cand, P, U, T(0), RedSlot{});
+			launch_force(cand, P, U, T(0), RedSlot{}, rows);
 			MESH_CUDA(cudaEventRecord(e0, c.stream));
 			for (int r = 0; r < 3; ++r)
-				launch_force(cand, P, U, T(0), RedSlot{});
+				launch_force(cand, P, U, T(0), RedSlot{}, rows);
 			MESH_CUDA(cudaEventRecord(e1, c.stream));
 			MESH_CUDA(cudaEventSynchronize(e1));
 			float ms = 0;
@@ -1149,6 +1212,12 @@ template <int GRP, class T, int ND> struct Ops
 	{
 		int v = choose_force(P, U);
 		launch_force(v, P, U, T(coef), kin ? *kin : RedSlot{});
+	}
+	static void hmc_tune(Field &P, Field const &U) { choose_force(P, U, true); }
+	static void hmc_momentum_step(Field &P, Field const &U, double coef, RedSlot *kin)
+	{
+		int v = choose_force(P, U, true);
+		launch_force(v, P, U, T(coef), kin ? *kin : RedSlot{}, true);
 	}
 	static void landau_functional(Field const &U, Field const &g, RedSlot out)
 	{
@@ -1216,7 +1285,8 @@ template <int GRP, class T, int ND> struct Ops
 		                           cshift,       site_op,       sum_real_trace, plaquette,      staple_sum,
 		                           wilson_deriv, reunitize,     evolve,         momentum_step,  landau_functional,
 		                           landau_theta, landau_deriv,  landau_or_half, reunit_exact,   alg_dot,
-		                           exp_apply,    axpy_alg,      gauge_transform, tune};
+		                           exp_apply,    axpy_alg,      gauge_transform, tune,
+		                           hmc_plaquette, hmc_evolve,   hmc_momentum_step, hmc_tune};
 		return &t;
 	}
 };

@@ -296,6 +296,22 @@ template <int NR> struct Soa<float, NR>
 		if constexpr (R & 1)
 			v[NR - 1] = ld1<CP>(tail + s);
 	}
+	// the first K reals (K a multiple of 4, K <= 4 N4): the leading float4 planes
+	template <int K, int CP = CACHE_DEFAULT>
+	__device__ __forceinline__ static void load_head(float const *__restrict__ base, int64_t V, int64_t s, float *v)
+	{
+		static_assert(K % 4 == 0 && K <= 4 * N4, "head must be whole float4 planes");
+		float4 const *p4 = reinterpret_cast<float4 const *>(base);
+#pragma unroll
+		for (int k = 0; k < K / 4; ++k)
+		{
+			float4 t = ld4<CP>(p4 + (k * V + s));
+			v[4 * k] = t.x;
+			v[4 * k + 1] = t.y;
+			v[4 * k + 2] = t.z;
+			v[4 * k + 3] = t.w;
+		}
+	}
 	template <int CP = CACHE_DEFAULT>
 	__device__ __forceinline__ static void store(float *__restrict__ base, int64_t V, int64_t s, float const *v)
 	{
@@ -330,6 +346,20 @@ template <int NR> struct Soa<double, NR>
 		}
 		if constexpr (NR & 1)
 			v[NR - 1] = ld1d<CP>(base + int64_t(2 * N2) * V + s);
+	}
+	// the first K reals (K even): the leading double2 planes
+	template <int K, int CP = CACHE_DEFAULT>
+	__device__ __forceinline__ static void load_head(double const *__restrict__ base, int64_t V, int64_t s, double *v)
+	{
+		static_assert(K % 2 == 0 && K <= 2 * N2, "head must be whole double2 planes");
+		double2 const *p2 = reinterpret_cast<double2 const *>(base);
+#pragma unroll
+		for (int k = 0; k < K / 2; ++k)
+		{
+			double2 t = ld2d<CP>(p2 + (k * V + s));
+			v[2 * k] = t.x;
+			v[2 * k + 1] = t.y;
+		}
 	}
 	template <int CP = CACHE_DEFAULT>
 	__device__ __forceinline__ static void store(double *__restrict__ base, int64_t V, int64_t s, double const *v)

@@ -293,6 +293,23 @@ def test_run_host_roundtrip(ctx, oracle):
     assert rel(host, h.U.export()) == 0.0
 
 
+@pytest.mark.parametrize("g", [2, 3])
+def test_trajectory_momentum_step_matches_generic(ctx, oracle, g):
+    """the trajectory's momentum step (SU(3) FP32 links read as rows 0, 1 with
+    row 2 rebuilt) against the generic one and the FP64 oracle"""
+    dims = [8, 8, 8, 8]
+    U64 = thermal(oracle, g, dims)
+    P64 = oracle.random_momenta(g, 2, dims, 5, 0)
+    h = mg.Hmc(ctx, g, 1, mg.Grid(dims), seed=1)
+    h.U.import_(U64.astype(np.float32))
+    h.P.import_(P64.astype(np.float32))
+    h.momentum_step(BETA[g], 0.1)
+    P_ref = momenta(ctx, g, 1, dims, P64.astype(np.float32))
+    mg.momentum_step(P_ref, h.U, BETA[g], 0.1)
+    assert rel(h.P.export(), P_ref.export()) < 2e-6
+    assert rel(h.P.export(), oracle.momentum_step(g, 2, dims, U64, P64, BETA[g], 0.1)) < TOL32
+
+
 def test_mixed_precision_error_vs_fp64(ctx, oracle):
     """FP32 links/momenta/force with FP64 sums against the FP64 oracle on the
     same supplied inputs: plaquette and dH errors."""
@@ -300,12 +317,16 @@ def test_mixed_precision_error_vs_fp64(ctx, oracle):
     U64 = thermal(oracle, 3, dims, ntraj=4)
     P64 = oracle.random_momenta(3, 2, dims, 11, 0)
     d = oracle.make_deltas("2mn", 0.5, 5)
-    _, ro = oracle.hmc_update(3, 2, dims, U64, P64, 5.7, d, 0.5)
+    U_new, ro = oracle.hmc_update(3, 2, dims, U64, P64, 5.7, d, 0.5)
     h = mg.Hmc(ctx, 3, 1, mg.Grid(dims), seed=1)
     h.U.import_(U64.astype(np.float32))
     rec = h.update_supplied(momenta(ctx, 3, 1, dims, P64.astype(np.float32)), 0.5, 5.7, d)
     assert abs(rec["dH"] - ro["dH"]) < 0.05
     assert rec["plaquette"] == pytest.approx(ro["plaq"], abs=1e-5)
+    # the trajectory reads SU(3) FP32 links as rows 0, 1 and rebuilds row 2:
+    # the links after it still agree with the FP64 oracle at the FP32 level
+    assert rec["accept"] == ro["accept"]
+    assert rel(h.U.export(), U_new) < 2e-5
 
 
 # ---------------------------------------------------------------------------
