@@ -93,9 +93,9 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per launch of the force kernel from the committed ncu
-    summary, scaled to the 32^4 launch (null when absent)."""
-    p = os.path.join(ROOT, "profiles", "momentum_step_su3_f32.md")
+    """DRAM bytes per launch of the fused MD-step kernel from the committed
+    ncu summary, scaled to the 32^4 launch (null when absent)."""
+    p = os.path.join(ROOT, "profiles", "md_step_su3_f32.md")
     try:
         for line in open(p):
             if line.startswith("dram_bytes_per_launch_32^4:"):
@@ -233,7 +233,9 @@ def run_ours(args):
     d = mg.make_deltas(WORKLOAD["scheme"], WORKLOAD["eps"], WORKLOAD["substeps"])
     n = len(d)
     n_u, n_p = deltas_counts(n)
-    launches_per_traj = 1 + n_u + n_p + 1 + 2  # refresh, link updates, momentum steps, plaquette, metropolis, copy
+    # refresh, the first link update, n_p momentum steps each fused with the
+    # link update after it, plaquette, metropolis, accept copy
+    launches_per_traj = 1 + 1 + n_p + 1 + 2
     h = mg.Hmc(ctx, WORKLOAD["group"], mg.F32, grid, seed=WORKLOAD["seed"] + rank)
     h.randomize_gauge_field()
     h.run(beta, d, args.therm, use_graph=True)
@@ -266,16 +268,29 @@ def run_ours(args):
     plaq = float(np.mean(hist["plaq_history"][args.therm:]))
     edH = float(np.mean(np.exp(-hist["deltaH_history"][args.therm:])))
 
-    # dominant kernel: the trajectory's fused momentum step (staples + force +
-    # P update), timed alone with CUDA events on the launching stream
+    # dominant kernel: the trajectory's fused MD step (staples + force + P
+    # update + the link update after it, one thread per site), timed alone
+    # with CUDA events on the launching stream; du = 0 leaves U unchanged.
+    # Algorithmic bytes per launch: one momentum step (|U| + 2|P|) and one
+    # link update (2|U| + |P|)
     _, Ub, Pb = sizes(dims)
     B_f = Ub + 2 * Pb
+    B_md = B_f + 2 * Ub + Pb
     U, P = h.U, h.P
     reps = 20
     for _ in range(3):
-        h.momentum_step(beta, 1e-9)
+        h.md_step(beta, 1e-9, 0.0)
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(reps):
+        h.md_step(beta, 1e-9, 0.0)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    t_md = f0.elapsed_time(f1) / reps / 1000.0
+    for _ in range(3):
+        h.momentum_step(beta, 1e-9)
+    torch.cuda.synchronize()
     f0.record(stream)
     for _ in range(reps):
         h.momentum_step(beta, 1e-9)
@@ -290,7 +305,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     t_evolve = ev0.elapsed_time(ev1) / reps / 1000.0
     peak, peak_kind = measured_peaks()
-    achieved = B_f / t_force / 1e9
+    achieved = B_md / t_md / 1e9
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -305,12 +320,15 @@ def run_ours(args):
            "physics": {"acceptance": acc, "plaquette_mean": plaq, "exp_minus_dH_mean": edH},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": ncu_traffic(),
-                        "kernel": "k_momentum_step_tiled<SU3,float,4,..,f32x2,rows01> (fused staples+force+momentum "
-                                  "update; links read as rows 0,1, row 2 rebuilt)",
-                        "algorithmic_bytes_per_launch": B_f, "avg_launch_ms": t_force * 1e3,
+                        "kernel": "k_momentum_step_site<SU3,float,4,..,f32x2,rows01,fused> (staples + force + "
+                                  "momentum update + the following link update, one thread per site; links read "
+                                  "as rows 0,1, row 2 rebuilt)",
+                        "algorithmic_bytes_per_launch": B_md, "avg_launch_ms": t_md * 1e3,
                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                         else "fallback 6.8 TB/s"},
-           "kernels": {"link_update_ms": t_evolve * 1e3,
+           "kernels": {"momentum_step_alone_ms": t_force * 1e3,
+                       "momentum_step_alone_GBps": B_f / t_force / 1e9,
+                       "link_update_ms": t_evolve * 1e3,
                        "link_update_GBps": (2 * Ub + Pb) / t_evolve / 1e9,
                        "trajectory_algorithmic_GB": algorithmic_bytes_per_traj(dims, n) / 1e9,
                        "trajectory_effective_GBps": algorithmic_bytes_per_traj(dims, n) / (ms / args.steps / 1e3)

@@ -230,6 +230,13 @@ int mesh_hmc_load(mesh_hmc h, const char *path);
  * and P with the trajectory's kernel (SU(3) FP32 links read as rows 0 and 1,
  * row 2 rebuilt; the autotuned launch variant): for timing and tests. */
 int mesh_hmc_momentum_step(mesh_hmc h, double beta, double delta);
+/* One momentum step of size dp followed by one link update of size du on the
+ * chain's own U and P: the inner pair of runHmd (hmc.h:38-59), i.e.
+ * P -= beta/(2 Nc) dp proj(U S), then U <- exp(du P) U (evolve, hmc.h:26-36).
+ * With FP32 fields on a lattice the thread-per-site kernel tiles, both run in
+ * the one fused kernel the trajectory uses (the links are written out of
+ * place and the chain's buffers swapped); otherwise as two kernels. */
+int mesh_hmc_md_step(mesh_hmc h, double beta, double dp, double du);
 /* runHmcUpdate (hmc.cpp:413-445): one trajectory, synchronous, record out */
 int mesh_hmc_update(mesh_hmc h, double beta, const double *deltas, int n, mesh_hmc_record *rec);
 /* One trajectory on caller-supplied momenta P0 (algebra field, copied, not

@@ -77,6 +77,7 @@ SIGNATURES = {
                               C.POINTER(C.c_uint64)]),
     "mesh_hmc_save": (_I, [_P, C.c_char_p]),
     "mesh_hmc_momentum_step": (_I, [_P, _D, _D]),
+    "mesh_hmc_md_step": (_I, [_P, _D, _D, _D]),
     "mesh_hmc_load": (_I, [_P, C.c_char_p]),
     "mesh_field_set_zero": (_I, [_P]),
     "mesh_field_set_unit": (_I, [_P]),
@@ -512,6 +513,12 @@ class Hmc:
     def momentum_step(self, beta: float, delta: float):
         """the trajectory's momentum step on the chain's own U and P"""
         _chk(load().mesh_hmc_momentum_step(self.h, beta, delta))
+
+    def md_step(self, beta: float, dp: float, du: float):
+        """one momentum step (dp) and the link update (du) after it on the
+        chain's own U and P, fused in one kernel where the trajectory fuses
+        them"""
+        _chk(load().mesh_hmc_md_step(self.h, beta, dp, du))
 
     def save(self, path: str):
         """checkpoint: links, trajectory counter and seed"""

@@ -209,7 +209,10 @@ void meshgb::field_export_host(Field const &f, void *host, size_t bytes) { expor
 struct mesh_hmc_s
 {
 	Context *ctx = nullptr;
-	mesh_field_s U, Unew, P;
+	// U: the chain's configuration; Unew: the proposal; Ut: the second buffer
+	// of the fused momentum-step + link-update kernels, which write the links
+	// out of place (Unew and Ut alternate)
+	mesh_field_s U, Unew, Ut, P;
 	uint64_t seed = 0;
 	HmcDev *d_dev = nullptr;
 	HmcRecordDev *d_hist = nullptr;
@@ -286,23 +289,33 @@ struct mesh_hmc_s
 			ops.random_momenta_dev(p, seed, &d_dev->traj, rs(K_OLD));
 		double coef0 = beta / (2.0 * group_nc(u.group));
 		int last_p = n >= 3 ? n - 2 : -1;
+		// the proposal: built in Unew (and Ut, when momentum steps are fused
+		// with the link updates after them)
+		Field *cur = &un, *spare = &Ut.f;
 		for (int i = 0; i < n; ++i)
 		{
 			if (i % 2 == 0)
-				ops.hmc_evolve(i == 0 ? u : un, un, p, deltas[i], i == n - 1);
+				ops.hmc_evolve(i == 0 ? u : *cur, *cur, p, deltas[i], i == n - 1);
 			else
 			{
 				RedSlot kin = rs(K_NEW);
-				ops.hmc_momentum_step(p, un, coef0 * deltas[i], i == last_p ? &kin : nullptr);
+				RedSlot *k = i == last_p ? &kin : nullptr;
+				if (i + 1 < n && ops.hmc_md_step(p, *cur, *spare, coef0 * deltas[i], deltas[i + 1], i + 1 == n - 1, k))
+				{
+					std::swap(cur, spare);
+					++i; // the link update i + 1 is done
+				}
+				else
+					ops.hmc_momentum_step(p, *cur, coef0 * deltas[i], k);
 			}
 		}
 		if (last_p < 0)
 			ops.norm2(p, rs(K_NEW));
-		ops.hmc_plaquette(un, rs(S_NEW));
+		ops.hmc_plaquette(*cur, rs(S_NEW));
 		double *res = d_res;
 		launch_metropolis(c, d_dev, d_hist, res + S_CUR, res + K_OLD, res + S_NEW, res + K_NEW, res + S_CUR, beta,
 		                  nplanes(u.nd) * double(u.geom.V), double(group_nc(u.group)), seed, uniform, d_flag);
-		launch_copy_if(c, u.d, un.d, u.bytes, d_flag);
+		launch_copy_if(c, u.d, cur->d, u.bytes, d_flag);
 		++count;
 	}
 
@@ -745,6 +758,7 @@ int mesh_hmc_create(mesh_ctx ctx, int group, int precision, int nd, int32_t cons
 		h->seed = seed;
 		create_field(c, MESH_GROUP, group, precision, nd, dims, nd, h->U.f);
 		create_field(c, MESH_GROUP, group, precision, nd, dims, nd, h->Unew.f);
+		create_field(c, MESH_GROUP, group, precision, nd, dims, nd, h->Ut.f);
 		create_field(c, MESH_ALGEBRA, group, precision, nd, dims, nd, h->P.f);
 		DeviceGuard dg(c.device);
 		MESH_CUDA(cudaMalloc(&h->d_dev, sizeof(HmcDev)));
@@ -786,6 +800,7 @@ int mesh_hmc_destroy(mesh_hmc h)
 		// the fields hold the chain's references to the context
 		destroy_field(h->U.f);
 		destroy_field(h->Unew.f);
+		destroy_field(h->Ut.f);
 		destroy_field(h->P.f);
 	}
 	delete h;
@@ -873,6 +888,30 @@ int mesh_hmc_momentum_step(mesh_hmc h, double beta, double delta)
 	});
 }
 
+int mesh_hmc_md_step(mesh_hmc h, double beta, double dp, double du)
+{
+	return api([&] {
+		require(h != nullptr, "null hmc");
+		DeviceGuard dg(h->ctx->device);
+		Field &U = h->U.f, &P = h->P.f;
+		auto const &ops = ops_for(U);
+		double coef = beta / (2.0 * group_nc(U.group)) * dp;
+		if (ops.hmc_md_step(P, U, h->Ut.f, coef, du, false, nullptr))
+		{
+			// the new links are in Ut: swap the buffers (a captured trajectory
+			// holds the old addresses, so it is dropped)
+			std::swap(U.d, h->Ut.f.d);
+			h->drop_graph();
+		}
+		else
+		{
+			ops.hmc_momentum_step(P, U, coef, nullptr);
+			ops.hmc_evolve(U, U, P, du, false);
+		}
+		h->S_valid = false;
+	});
+}
+
 static void copy_rec(HmcRecordDev const &r, mesh_hmc_record *rec)
 {
 	if (!rec)
@@ -940,6 +979,7 @@ int mesh_hmc_run(mesh_hmc h, double beta, double const *deltas, int n, int count
 		}
 		// choose launch variants before capturing (tuning times kernels)
 		ops_for(h->U.f).hmc_tune(h->P.f, h->Unew.f);
+		ops_for(h->U.f).hmc_tune_md(h->P.f, h->Unew.f, h->Ut.f);
 		std::vector<double> dv(deltas, deltas + n);
 		if (!h->graph || h->graph_beta != beta || h->graph_deltas != dv || h->graph_hist != h->d_hist)
 		{

@@ -113,6 +113,12 @@ struct OpsTable
 	void (*hmc_evolve)(Field const &Usrc, Field &Udst, Field const &P, double t, bool reunit);
 	void (*hmc_momentum_step)(Field &P, Field const &U, double coef, RedSlot *kin);
 	void (*hmc_tune)(Field &P, Field const &U);
+	// the trajectory's momentum step fused with the link update after it:
+	// P -= coef F(Uin), Uout = exp(tu P) Uin (reunitised when `reunit`);
+	// returns false, launching nothing, where the fused kernel does not apply
+	// (then the two steps run separately)
+	bool (*hmc_md_step)(Field &P, Field const &Uin, Field &Uout, double coef, double tu, bool reunit, RedSlot *kin);
+	void (*hmc_tune_md)(Field &P, Field const &Uin, Field &Uout);
 };
 
 // autotuning registry (tune.cu): variant index per kernel/lattice key

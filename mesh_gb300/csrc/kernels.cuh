@@ -459,6 +459,201 @@ __global__ void __launch_bounds__(NT, MINB)
 		grid_sum<NT>(acc, kin);
 }
 
+// site t of tile `tile` (TileSpec order: tiles lexicographic, sites of a tile
+// lexicographic with the last dimension fastest)
+template <int ND> __device__ __forceinline__ void tile_site(TileSpec const &ts, int tile, int t, int *x)
+{
+	int r = tile;
+#pragma unroll
+	for (int i = ND - 1; i >= 0; --i)
+	{
+		int q = r / ts.nt[i];
+		x[i] = ((r - q * ts.nt[i]) << ts.lt[i]) + (t & ((1 << ts.lt[i]) - 1));
+		t >>= ts.lt[i];
+		r = q;
+	}
+}
+
+// planes mu < nu numbered q = 0 .. ND(ND-1)/2 - 1 in the order (0,1), (0,2), ...
+template <int ND> __host__ __device__ constexpr int plane_mu(int q)
+{
+	int mu = 0;
+	while (q >= ND - 1 - mu)
+	{
+		q -= ND - 1 - mu;
+		++mu;
+	}
+	return mu;
+}
+template <int ND> __host__ __device__ constexpr int plane_nu(int q)
+{
+	int mu = 0;
+	while (q >= ND - 1 - mu)
+	{
+		q -= ND - 1 - mu;
+		++mu;
+	}
+	return mu + 1 + q;
+}
+
+// F[mu] += x, F[nu] -= x for the plane q (a runtime index): a chain of
+// branches on compile-time planes keeps F in registers
+template <int ND, int NA, int K = 0, class T>
+__device__ __forceinline__ void add_plane(T (&F)[ND][NA], int q, T const *x)
+{
+	if constexpr (K < ND * (ND - 1) / 2)
+	{
+		if (q == K)
+		{
+			constexpr int mu = plane_mu<ND>(K), nu = plane_nu<ND>(K);
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+			{
+				F[mu][a] += x[a];
+				F[nu][a] -= x[a];
+			}
+		}
+		else
+			add_plane<ND, NA, K + 1>(F, q, x);
+	}
+}
+template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F)[ND][NA], int mu, T const *x)
+{
+#pragma unroll
+	for (int k = 0; k < ND; ++k)
+		if (k == mu)
+		{
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				F[k][a] += x[a];
+		}
+}
+
+// Momentum step, one thread per site updating the momenta of all ND links of
+// the site. With a = U_mu(x), b = U_nu(x+mu), c = U_mu(x+nu), d = U_nu(x),
+// the forward staple of link (x, mu) in the plane (mu, nu) closes to the
+// plaquette loop a b c^+ d^+ = (a b)(d c)^+ and the forward staple of link
+// (x, nu) in the same plane closes to its adjoint, whose projection is the
+// negative: both come from 3 products. The backward staples are summed per
+// direction and multiplied by U_mu(x) once, as in staple(). For SU(3) that is
+// 11.5 matrix products and 11 link loads per link, against 13 products and 19
+// loads when each link is handled on its own. The sum over staples runs in a
+// different order than the reference's (forward loops first), which changes
+// results only at the rounding level.
+//
+// FUSE: the link update that follows the momentum step in the integrator is
+// done in the same pass, out of place: Uout_mu(x) = exp(tu P_mu(x)) U_mu(x)
+// with the updated momentum (and project_on_group_fast when `reunit`), which
+// saves the separate link-update kernel's reads of U and P. The force of every
+// link reads U only, so writing Uout is race free.
+template <int GRP, class T, int ND, int NT, int MINB, bool F2 = false, bool ROWS = false, bool FUSE = false>
+__global__ void __launch_bounds__(NT, MINB)
+    k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
+                         T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	using Pr = Prod<GRP, T, F2>;
+	constexpr int NA = Gp::NA;
+	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
+	double acc = 0.0;
+	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
+	{
+		for (int t = threadIdx.x; t < ts.sites; t += NT)
+		{
+			int x[ND];
+			tile_site<ND>(ts, tile, t, x);
+			Site<ND> st = site_from_coords<ND>(g, x);
+			int64_t s = eo_of<ND>(g, st);
+			T F[ND][NA];
+#pragma unroll
+			for (int mu = 0; mu < ND; ++mu)
+#pragma unroll
+				for (int a = 0; a < NA; ++a)
+					F[mu][a] = T(0);
+			// forward plaquette loops, one per plane
+#pragma unroll 1
+			for (int q = 0; q < ND * (ND - 1) / 2; ++q)
+			{
+				int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
+				E ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+				E dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+				E pl = Pr::mul_nd(ab, dc);
+				T xa[NA];
+				Gp::proj(pl, xa);
+				add_plane<ND, NA>(F, q, xa);
+			}
+			// backward staples
+#pragma unroll 1
+			for (int mu = 0; mu < ND; ++mu)
+			{
+				E S = Gp::zero();
+#pragma unroll 1
+				for (int nu = 0; nu < ND; ++nu)
+				{
+					if (nu == mu)
+						continue;
+					int64_t y = eo_shift1<ND>(g, st, nu, -1);
+					E e = ld(mu, y);
+					E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
+					E h = ld(nu, y);
+					Gp::add_to(S, Pr::mul_dn(Pr::mul(e, f), h));
+				}
+				E W = Pr::mul(ld(mu, s), S);
+				T xa[NA];
+				Gp::proj(W, xa);
+				add_dir<ND, NA>(F, mu, xa);
+			}
+			if constexpr (!FUSE)
+			{
+#pragma unroll
+				for (int mu = 0; mu < ND; ++mu)
+				{
+					auto Pv = comp<T, NA>(P, g.V, mu);
+					T p[NA];
+					Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+					for (int a = 0; a < NA; ++a)
+						p[a] -= coef * F[mu][a];
+					Pv.template store<CACHE_STREAM>(s, p);
+					acc += double(Gp::kin(p));
+				}
+			}
+			else
+			{
+				// one copy of the exp body: rolled direction loop
+#pragma unroll 1
+				for (int mu = 0; mu < ND; ++mu)
+				{
+					T f[NA];
+#pragma unroll
+					for (int a = 0; a < NA; ++a)
+					{
+						f[a] = F[0][a];
+#pragma unroll
+						for (int k = 1; k < ND; ++k)
+							f[a] = mu == k ? F[k][a] : f[a];
+					}
+					auto Pv = comp<T, NA>(P, g.V, mu);
+					T p[NA];
+					Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+					for (int a = 0; a < NA; ++a)
+						p[a] -= coef * f[a];
+					Pv.template store<CACHE_STREAM>(s, p);
+					acc += double(Gp::kin(p));
+					E r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
+					if (reunit)
+						r = Gp::reunit_fast(r);
+					comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
+				}
+			}
+		}
+	}
+	if (kin.result)
+		grid_sum<NT>(acc, kin);
+}
+
 template <int GRP, class T, int ND>
 __global__ void __launch_bounds__(kBlock) k_staple_sum(Geom g, int mu, T const *__restrict__ U, T *__restrict__ S)
 {
@@ -1053,28 +1248,44 @@ template <int GRP, class T, int ND> struct Ops
 		bool f2 = false; // packed FP32x2 products (SU(3) float only)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
-	static int n_force_variants() { return ND == 4 ? (kF2 ? 14 : 11) : 2; }
+	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
+	// packed FP32x2 products; 14-17: thread per site (k_momentum_step_site)
+	// with FP32x2 products; 18-20: thread per site, plain products
+	static constexpr int kForceVariants = 21;
+	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
-		static const ForceVariant t[11] = {
-		    {0, {0, 0, 0, 0}, 256, 1, "eo-order/256thr/1blk"},    {0, {0, 0, 0, 0}, 256, 2, "eo-order/256thr/2blk"},
-		    {1, {2, 2, 2, 2}, 256, 1, "tile4x4x4x4/256thr/1blk"},  {1, {2, 2, 2, 2}, 256, 2, "tile4x4x4x4/256thr/2blk"},
-		    {1, {1, 2, 2, 2}, 128, 3, "tile2x4x4x4/128thr/3blk"},  {1, {1, 2, 2, 2}, 128, 4, "tile2x4x4x4/128thr/4blk"},
-		    {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk"},  {1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk"},
-		    {1, {1, 1, 1, 3}, 128, 4, "tile2x2x2x8/128thr/4blk"},  {1, {1, 1, 2, 4}, 128, 4, "tile2x2x4x16/128thr/4blk"},
-		    {1, {0, 1, 2, 4}, 128, 4, "tile1x2x4x16/128thr/4blk"}};
-		if (v >= 11)
-		{
-			static const ForceVariant f[3] = {{1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk/f32x2", true},
-			                                  {1, {1, 1, 2, 3}, 128, 3, "tile2x2x4x8/128thr/3blk/f32x2", true},
-			                                  {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk/f32x2", true}};
-			return f[v - 11];
-		}
+		static const ForceVariant t[kForceVariants] = {
+		    {0, {0, 0, 0, 0}, 256, 1, "eo-order/256thr/1blk"},
+		    {0, {0, 0, 0, 0}, 256, 2, "eo-order/256thr/2blk"},
+		    {1, {2, 2, 2, 2}, 256, 1, "tile4x4x4x4/256thr/1blk"},
+		    {1, {2, 2, 2, 2}, 256, 2, "tile4x4x4x4/256thr/2blk"},
+		    {1, {1, 2, 2, 2}, 128, 3, "tile2x4x4x4/128thr/3blk"},
+		    {1, {1, 2, 2, 2}, 128, 4, "tile2x4x4x4/128thr/4blk"},
+		    {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk"},
+		    {1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk"},
+		    {1, {1, 1, 1, 3}, 128, 4, "tile2x2x2x8/128thr/4blk"},
+		    {1, {1, 1, 2, 4}, 128, 4, "tile2x2x4x16/128thr/4blk"},
+		    {1, {0, 1, 2, 4}, 128, 4, "tile1x2x4x16/128thr/4blk"},
+		    {1, {1, 1, 2, 3}, 128, 4, "tile2x2x4x8/128thr/4blk/f32x2", true},
+		    {1, {1, 1, 2, 3}, 128, 3, "tile2x2x4x8/128thr/3blk/f32x2", true},
+		    {1, {2, 2, 2, 3}, 256, 2, "tile4x4x4x8/256thr/2blk/f32x2", true},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2", true},
+		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk/f32x2", true},
+		    {2, {1, 2, 2, 3}, 256, 2, "site/tile2x4x4x8/256thr/2blk/f32x2", true},
+		    {2, {0, 1, 2, 4}, 128, 4, "site/tile1x2x4x16/128thr/4blk/f32x2", true},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk"},
+		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk"},
+		    {2, {1, 2, 2, 3}, 256, 2, "site/tile2x4x4x8/256thr/2blk"}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
 	{
+		if (v < 0 || v >= n_force_variants())
+			return false;
 		ForceVariant fv = force_variant(v);
+		if (fv.f2 && !kF2)
+			return false;
 		if (!fv.tiled)
 			return true;
 		if (ND != 4)
@@ -1111,19 +1322,11 @@ template <int GRP, class T, int ND> struct Ops
 		}
 		else if constexpr (ND == 4)
 		{
-			TileSpec ts{};
-			ts.sites = 1;
-			ts.ntiles = 1;
-			for (int i = 0; i < 4; ++i)
-			{
-				ts.lt[i] = fv.lt[i];
-				ts.nt[i] = g.L[i] >> fv.lt[i];
-				ts.sites <<= fv.lt[i];
-				ts.ntiles *= ts.nt[i];
-			}
-			int64_t cap = int64_t(c.num_sms) * fv.minb;
-			unsigned b = unsigned(ts.ntiles < cap ? ts.ntiles : cap);
-			if (fv.f2)
+			unsigned b = 0;
+			TileSpec ts = tiles_for(g, fv, c, b);
+			if (fv.tiled == 2)
+				launch_force_site<ROWS>(fv, b, g, ts, u, p, coef, kin, c);
+			else if (fv.f2)
 			{
 				if constexpr (kF2)
 				{
@@ -1148,6 +1351,171 @@ template <int GRP, class T, int ND> struct Ops
 				k_momentum_step_tiled<GRP, T, 4, 128, 4, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
 		}
 		MESH_LAUNCH_CHECK();
+	}
+	template <bool ROWS>
+	static void launch_force_site(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u,
+	                              T *p, T coef, RedSlot kin, Context &c)
+	{
+		if constexpr (ND == 4)
+		{
+			if (fv.f2)
+			{
+				if constexpr (kF2)
+				{
+					if (fv.threads == 128 && fv.minb == 4)
+						k_momentum_step_site<GRP, T, 4, 128, 4, true, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+					else if (fv.threads == 128)
+						k_momentum_step_site<GRP, T, 4, 128, 3, true, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+					else
+						k_momentum_step_site<GRP, T, 4, 256, 2, true, ROWS><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				}
+			}
+			else if (fv.threads == 128 && fv.minb == 4)
+				k_momentum_step_site<GRP, T, 4, 128, 4, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+			else if (fv.threads == 128)
+				k_momentum_step_site<GRP, T, 4, 128, 3, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+			else
+				k_momentum_step_site<GRP, T, 4, 256, 2, false, ROWS><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+		}
+	}
+	// tiles of variant fv over g and the grid size (at most minb blocks per SM)
+	static TileSpec tiles_for(Geom const &g, ForceVariant const &fv, Context const &c, unsigned &b)
+	{
+		TileSpec ts{};
+		ts.sites = 1;
+		ts.ntiles = 1;
+		for (int i = 0; i < 4; ++i)
+		{
+			ts.lt[i] = fv.lt[i];
+			ts.nt[i] = g.L[i] >> fv.lt[i];
+			ts.sites <<= fv.lt[i];
+			ts.ntiles *= ts.nt[i];
+		}
+		int64_t cap = int64_t(c.num_sms) * fv.minb;
+		b = unsigned(ts.ntiles < cap ? ts.ntiles : cap);
+		return ts;
+	}
+	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
+	static constexpr int kMdFirst = 14, kMdLast = 20; // the thread-per-site variants
+	static bool md_supported(Geom const &g)
+	{
+		if constexpr (ND != 4 || sizeof(T) != 4)
+			return false;
+		for (int v = kMdFirst; v <= kMdLast; ++v)
+			if (force_variant_valid(g, v))
+				return true;
+		return false;
+	}
+	static void launch_md(int v, Field &P, Field const &Uin, Field &Uout, T coef, T tu, int reunit, RedSlot kin)
+	{
+		if constexpr (ND == 4)
+		{
+			constexpr bool R = kRows<GRP, T>;
+			auto &c = *Uin.ctx;
+			Geom const &g = Uin.geom;
+			ForceVariant fv = force_variant(v);
+			unsigned b = 0;
+			TileSpec ts = tiles_for(g, fv, c, b);
+			T const *u = static_cast<T const *>(Uin.d);
+			T *p = static_cast<T *>(P.d);
+			T *uo = static_cast<T *>(Uout.d);
+			if (fv.f2)
+			{
+				if constexpr (kF2)
+				{
+					if (fv.threads == 128 && fv.minb == 4)
+						k_momentum_step_site<GRP, T, 4, 128, 4, true, R, true>
+						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+					else if (fv.threads == 128)
+						k_momentum_step_site<GRP, T, 4, 128, 3, true, R, true>
+						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+					else
+						k_momentum_step_site<GRP, T, 4, 256, 2, true, R, true>
+						    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				}
+			}
+			else if (fv.threads == 128 && fv.minb == 4)
+				k_momentum_step_site<GRP, T, 4, 128, 4, false, R, true>
+				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+			else if (fv.threads == 128)
+				k_momentum_step_site<GRP, T, 4, 128, 3, false, R, true>
+				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+			else
+				k_momentum_step_site<GRP, T, 4, 256, 2, false, R, true>
+				    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+			MESH_LAUNCH_CHECK();
+		}
+	}
+	// fastest thread-per-site variant of the fused step for this lattice, timed
+	// once with coef = 0 and tu = 0 (P unchanged, Uout = Uin); not while the
+	// stream is capturing
+	static int choose_md(Field &P, Field const &Uin, Field &Uout)
+	{
+		int ov = force_override();
+		if (ov >= kMdFirst && ov <= kMdLast && force_variant_valid(Uin.geom, ov))
+			return ov;
+		std::string key = "md_step/group" + std::to_string(GRP) + "/" + (sizeof(T) == 4 ? "f32" : "f64") + "/";
+		for (int i = 0; i < ND; ++i)
+			key += (i ? "x" : "") + std::to_string(Uin.dims[i]);
+		int v = tuned_variant(key);
+		if (v >= 0)
+			return v;
+		int dflt = -1;
+		for (int cand = kMdFirst; cand <= kMdLast && dflt < 0; ++cand)
+			if (force_variant_valid(Uin.geom, cand))
+				dflt = cand;
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		cudaStreamIsCapturing(Uin.ctx->stream, &cs);
+		if (cs != cudaStreamCaptureStatusNone || !autotune_enabled())
+			return dflt;
+		auto &c = *Uin.ctx;
+		cudaEvent_t e0, e1;
+		MESH_CUDA(cudaEventCreate(&e0));
+		MESH_CUDA(cudaEventCreate(&e1));
+		float best = 1e30f;
+		int bestv = dflt;
+		std::string report;
+		for (int cand = kMdFirst; cand <= kMdLast; ++cand)
+		{
+			if (!force_variant_valid(Uin.geom, cand))
+				continue;
+			launch_md(cand, P, Uin, Uout, T(0), T(0), 0, RedSlot{});
+			MESH_CUDA(cudaEventRecord(e0, c.stream));
+			for (int r = 0; r < 3; ++r)
+				launch_md(cand, P, Uin, Uout, T(0), T(0), 0, RedSlot{});
+			MESH_CUDA(cudaEventRecord(e1, c.stream));
+			MESH_CUDA(cudaEventSynchronize(e1));
+			float ms = 0;
+			MESH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+			ms /= 3;
+			report += std::string(report.empty() ? "" : ", ") + force_variant(cand).name + "=" +
+			          std::to_string(ms * 1000.0f) + "us";
+			if (ms < best)
+			{
+				best = ms;
+				bestv = cand;
+			}
+		}
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		set_tuned_variant(key, bestv, std::string("chosen ") + force_variant(bestv).name + " [" + report + "]");
+		return bestv;
+	}
+	// momentum step P -= coef F(Uin) fused with the link update
+	// Uout = exp(tu P) Uin; false (nothing launched) where no fused variant fits
+	static bool hmc_md_step(Field &P, Field const &Uin, Field &Uout, double coef, double tu, bool reunit,
+	                        RedSlot *kin)
+	{
+		if (!md_supported(Uin.geom))
+			return false;
+		int v = choose_md(P, Uin, Uout);
+		launch_md(v, P, Uin, Uout, T(coef), T(tu), reunit ? 1 : 0, kin ? *kin : RedSlot{});
+		return true;
+	}
+	static void hmc_tune_md(Field &P, Field const &Uin, Field &Uout)
+	{
+		if (md_supported(Uin.geom))
+			choose_md(P, Uin, Uout);
 	}
 	static std::string force_key(Field const &U, bool rows)
 	{
@@ -1286,7 +1654,8 @@ template <int GRP, class T, int ND> struct Ops
 		                           wilson_deriv, reunitize,     evolve,         momentum_step,  landau_functional,
 		                           landau_theta, landau_deriv,  landau_or_half, reunit_exact,   alg_dot,
 		                           exp_apply,    axpy_alg,      gauge_transform, tune,
-		                           hmc_plaquette, hmc_evolve,   hmc_momentum_step, hmc_tune};
+		                           hmc_plaquette, hmc_evolve,   hmc_momentum_step, hmc_tune,
+		                           hmc_md_step,   hmc_tune_md};
 		return &t;
 	}
 };

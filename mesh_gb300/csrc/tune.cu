@@ -1,7 +1,8 @@
 // Autotuner registry: the launch variant chosen per (kernel, group,
 // precision, lattice) key, measured once per process with CUDA events on the
 // context's stream (kernels.cuh, Ops::choose_force). MESH_AUTOTUNE=0 in the
-// environment disables timing and uses the default variants.
+// environment disables timing and uses the default variants;
+// MESH_FORCE_VARIANT=v pins momentum-step variant v where it is valid.
 #include "field.cuh"
 
 #include <cstdlib>
@@ -32,9 +33,19 @@ void set_tuned_variant(std::string const &key, int variant, std::string const &r
 }
 
 namespace {
-int g_force_override = -1;
+int g_force_override = -2; // -2: not yet read from MESH_FORCE_VARIANT
 }
-int force_override() { return g_force_override; }
+// the variant pinned by mesh_tune_force_variant, else by MESH_FORCE_VARIANT in
+// the environment (read once), else -1 (autotune)
+int force_override()
+{
+	if (g_force_override == -2)
+	{
+		char const *e = std::getenv("MESH_FORCE_VARIANT");
+		g_force_override = e && *e ? std::atoi(e) : -1;
+	}
+	return g_force_override;
+}
 void set_force_override(int v) { g_force_override = v; }
 
 bool autotune_enabled()

@@ -177,10 +177,11 @@ def test_staples_force_evolve_reunit_vs_oracle(ctx, oracle, g, p):
     assert rel(P.export(), oracle.momentum_step(g, 2, dims, U64, P64, BETA[g], 0.05)) < tol(p)
 
 
-@pytest.mark.parametrize("variant", list(range(14)))
+@pytest.mark.parametrize("variant", list(range(21)))
 @pytest.mark.parametrize("g,p", [(3, 1), (3, 2), (2, 1), (1, 1)])
 def test_every_force_launch_variant_vs_oracle(ctx, oracle, g, p, variant):
-    """each launch variant the autotuner can choose (even/odd order, 4D tiles,
+    """each launch variant the autotuner can choose (thread per link in
+    even/odd order or 4D tiles, thread per site with shared plaquette loops,
     packed FP32x2 products) computes the same momentum step"""
     dims = [8, 8, 8, 16]
     U64 = thermal(oracle, g, dims, ntraj=1)
@@ -293,34 +294,75 @@ def test_run_host_roundtrip(ctx, oracle):
     assert rel(host, h.U.export()) == 0.0
 
 
+@pytest.mark.parametrize("variant", [-1, 11, 13, 14, 15, 16, 17, 18, 20])
 @pytest.mark.parametrize("g", [2, 3])
-def test_trajectory_momentum_step_matches_generic(ctx, oracle, g):
+def test_trajectory_momentum_step_matches_generic(ctx, oracle, g, variant):
     """the trajectory's momentum step (SU(3) FP32 links read as rows 0, 1 with
-    row 2 rebuilt) against the generic one and the FP64 oracle"""
+    row 2 rebuilt), in every launch variant, against the generic one and the
+    FP64 oracle"""
     dims = [8, 8, 8, 8]
     U64 = thermal(oracle, g, dims)
     P64 = oracle.random_momenta(g, 2, dims, 5, 0)
     h = mg.Hmc(ctx, g, 1, mg.Grid(dims), seed=1)
     h.U.import_(U64.astype(np.float32))
     h.P.import_(P64.astype(np.float32))
-    h.momentum_step(BETA[g], 0.1)
+    try:
+        mg.force_variant(variant)
+        h.momentum_step(BETA[g], 0.1)
+    finally:
+        mg.force_variant(-1)
     P_ref = momenta(ctx, g, 1, dims, P64.astype(np.float32))
     mg.momentum_step(P_ref, h.U, BETA[g], 0.1)
     assert rel(h.P.export(), P_ref.export()) < 2e-6
     assert rel(h.P.export(), oracle.momentum_step(g, 2, dims, U64, P64, BETA[g], 0.1)) < TOL32
 
 
-def test_mixed_precision_error_vs_fp64(ctx, oracle):
+@pytest.mark.parametrize("g,p", [(3, 1), (2, 1), (1, 1), (3, 2)])
+def test_md_step_vs_oracle(ctx, oracle, g, p):
+    """the momentum step fused with the link update after it (FP32: one
+    thread-per-site kernel; FP64: the two kernels) against the oracle's
+    momentum step followed by evolve"""
+    dims = [8, 8, 8, 16]
+    U64 = thermal(oracle, g, dims)
+    P64 = oracle.random_momenta(g, 2, dims, 5, 0)
+    dt = mg.real_dtype(p)
+    h = mg.Hmc(ctx, g, p, mg.Grid(dims), seed=1)
+    h.U.import_(U64.astype(dt))
+    h.P.import_(P64.astype(dt))
+    h.md_step(BETA[g], 0.1, 0.07)
+    P_o = oracle.momentum_step(g, 2, dims, U64, P64, BETA[g], 0.1)
+    U_o = oracle.evolve(g, 2, dims, U64, P_o, 0.07)
+    assert rel(h.P.export(), P_o) < tol(p)
+    assert rel(h.U.export(), U_o) < tol(p)
+    # a second step from the swapped buffers
+    h.md_step(BETA[g], 0.1, 0.07)
+    P_o = oracle.momentum_step(g, 2, dims, U_o, P_o, BETA[g], 0.1)
+    U_o = oracle.evolve(g, 2, dims, U_o, P_o, 0.07)
+    assert rel(h.P.export(), P_o) < 2 * tol(p)
+    assert rel(h.U.export(), U_o) < 2 * tol(p)
+
+
+MD_VARIANTS = [(3, v) for v in (-1, 14, 15, 16, 17, 18, 19, 20)] + [(g, v) for g in (1, 2) for v in (-1, 18, 20)]
+
+
+@pytest.mark.parametrize("g,variant", MD_VARIANTS)
+def test_mixed_precision_error_vs_fp64(ctx, oracle, g, variant):
     """FP32 links/momenta/force with FP64 sums against the FP64 oracle on the
-    same supplied inputs: plaquette and dH errors."""
+    same supplied inputs: plaquette and dH errors. On this lattice every
+    momentum step of the trajectory runs fused with the link update after it
+    (thread-per-site kernel, each launch variant pinned in turn)."""
     dims = [8, 8, 8, 8]
-    U64 = thermal(oracle, 3, dims, ntraj=4)
-    P64 = oracle.random_momenta(3, 2, dims, 11, 0)
+    U64 = thermal(oracle, g, dims, ntraj=4)
+    P64 = oracle.random_momenta(g, 2, dims, 11, 0)
     d = oracle.make_deltas("2mn", 0.5, 5)
-    U_new, ro = oracle.hmc_update(3, 2, dims, U64, P64, 5.7, d, 0.5)
-    h = mg.Hmc(ctx, 3, 1, mg.Grid(dims), seed=1)
+    U_new, ro = oracle.hmc_update(g, 2, dims, U64, P64, BETA[g], d, 0.5)
+    h = mg.Hmc(ctx, g, 1, mg.Grid(dims), seed=1)
     h.U.import_(U64.astype(np.float32))
-    rec = h.update_supplied(momenta(ctx, 3, 1, dims, P64.astype(np.float32)), 0.5, 5.7, d)
+    try:
+        mg.force_variant(variant)
+        rec = h.update_supplied(momenta(ctx, g, 1, dims, P64.astype(np.float32)), 0.5, BETA[g], d)
+    finally:
+        mg.force_variant(-1)
     assert abs(rec["dH"] - ro["dH"]) < 0.05
     assert rec["plaquette"] == pytest.approx(ro["plaq"], abs=1e-5)
     # the trajectory reads SU(3) FP32 links as rows 0, 1 and rebuilds row 2:
