@@ -389,6 +389,52 @@ template <class T> struct Group<SU3, T>
 		r = csub(r, cmul(m.at(0, 1), csub(c, d)));
 		return cadd(r, cmul(m.at(0, 2), csub(e, f)));
 	}
+	// exp(X) for antihermitian traceless X with |X| < 1 (Frobenius norm), as
+	// the power series truncated after X^10 (remainder below |X|^11/11! =
+	// 2.5e-8) and reduced to a polynomial u0 + u1 X + u2 X^2 with the
+	// Cayley-Hamilton relation X^3 = -c1 X + i dim, c1 = |X|^2/2,
+	// i dim = det X; the series is summed by Horner's rule on the three
+	// coefficients (M. Luscher, "SU(3) matrix functions", openQCD notes). No
+	// transcendental functions: the FP32 trajectory's link update.
+	MESH_HD static E exp_series(E const &X, E const &X2, T c1, T dim)
+	{
+		constexpr int N = 10;
+		// 1/k! for k = 0..N
+		constexpr T inv_fact[N + 1] = {T(1),
+		                               T(1),
+		                               T(1.0 / 2),
+		                               T(1.0 / 6),
+		                               T(1.0 / 24),
+		                               T(1.0 / 120),
+		                               T(1.0 / 720),
+		                               T(1.0 / 5040),
+		                               T(1.0 / 40320),
+		                               T(1.0 / 362880),
+		                               T(1.0 / 3628800)};
+		cx<T> u0 = {inv_fact[N], T(0)}, u1 = {T(0), T(0)}, u2 = {T(0), T(0)};
+#pragma unroll
+		for (int k = N - 1; k >= 0; --k)
+		{
+			// X (u0 + u1 X + u2 X^2) + 1/k! = (i dim u2 + 1/k!) + (u0 - c1 u2) X + u1 X^2
+			cx<T> n0 = {inv_fact[k] - dim * u2.im, dim * u2.re};
+			cx<T> n1 = {u0.re - c1 * u2.re, u0.im - c1 * u2.im};
+			u2 = u1;
+			u1 = n1;
+			u0 = n0;
+		}
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				cx<T> z = cadd(cmul(u1, X.at(i, j)), cmul(u2, X2.at(i, j)));
+				if (i == j)
+					z = cadd(z, u0);
+				r.set(i, j, z);
+			}
+		return r;
+	}
 	// exp(t X) for X = from_alg(o) (antihermitian traceless), Cayley-Hamilton
 	MESH_HD static E exp_alg(T const *o, T t)
 	{
@@ -401,6 +447,9 @@ template <class T> struct Group<SU3, T>
 		// c1 = Tr(Q^2)/2 = |X|^2/2,  c0 = det(Q) = det(-iX) = -Im det(X)
 		T c1 = T(0.5) * kin(x);
 		T c0 = -det(X).im;
+		if constexpr (sizeof(T) == 4)
+			if (c1 < T(0.5))
+				return exp_series(X, X2, c1, -c0);
 		cx<T> f0, f1, f2;
 		T const tiny = sizeof(T) == 8 ? T(1e-11) : T(1e-5);
 		if (c1 < tiny)

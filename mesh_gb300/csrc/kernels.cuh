@@ -1249,9 +1249,10 @@ template <int GRP, class T, int ND> struct Ops
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
-	// packed FP32x2 products; 14-17: thread per site (k_momentum_step_site)
-	// with FP32x2 products; 18-20: thread per site, plain products
-	static constexpr int kForceVariants = 21;
+	// packed FP32x2 products; 14-17 and 21-22: thread per site
+	// (k_momentum_step_site) with FP32x2 products; 18-20: thread per site,
+	// plain products
+	static constexpr int kForceVariants = 23;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1276,7 +1277,9 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 1, 2, 4}, 128, 4, "site/tile1x2x4x16/128thr/4blk/f32x2", true},
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk"},
 		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk"},
-		    {2, {1, 2, 2, 3}, 256, 2, "site/tile2x4x4x8/256thr/2blk"}};
+		    {2, {1, 2, 2, 3}, 256, 2, "site/tile2x4x4x8/256thr/2blk"},
+		    {2, {2, 2, 2, 3}, 512, 1, "site/tile4x4x4x8/512thr/1blk/f32x2", true},
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2", true}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1362,7 +1365,9 @@ template <int GRP, class T, int ND> struct Ops
 			{
 				if constexpr (kF2)
 				{
-					if (fv.threads == 128 && fv.minb == 4)
+					if (fv.threads == 512)
+						k_momentum_step_site<GRP, T, 4, 512, 1, true, ROWS><<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin);
+					else if (fv.threads == 128 && fv.minb == 4)
 						k_momentum_step_site<GRP, T, 4, 128, 4, true, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
 					else if (fv.threads == 128)
 						k_momentum_step_site<GRP, T, 4, 128, 3, true, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
@@ -1396,7 +1401,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
-	static constexpr int kMdFirst = 14, kMdLast = 20; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 22; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4 || sizeof(T) != 4)
@@ -1423,7 +1428,10 @@ template <int GRP, class T, int ND> struct Ops
 			{
 				if constexpr (kF2)
 				{
-					if (fv.threads == 128 && fv.minb == 4)
+					if (fv.threads == 512)
+						k_momentum_step_site<GRP, T, 4, 512, 1, true, R, true>
+						    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+					else if (fv.threads == 128 && fv.minb == 4)
 						k_momentum_step_site<GRP, T, 4, 128, 4, true, R, true>
 						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 					else if (fv.threads == 128)
