@@ -95,15 +95,36 @@ HIGHS = (1.0, 0.5, 0.35, 0.2)
 TABLE_N = 256
 
 
-def family_mult(alpha, high, p2, p2min, p2max):
-    w = np.clip(np.log(4.0 * p2 / p2max) / np.log(4.0), 0.0, 1.0)
-    return alpha * p2max / p2 * high ** w
+def family_mult(alpha, high, p2, p2min, p2max, low=1.0):
+    """alpha p2max/p^2 high^w_hi low^w_lo: w_hi ramps (in log p^2) from 0 at
+    p2max/4 to 1 at p2max, w_lo from 1 at p2min to 0 at 4 p2min"""
+    w_hi = np.clip(np.log(4.0 * p2 / p2max) / np.log(4.0), 0.0, 1.0)
+    w_lo = np.clip(np.log(4.0 * p2min / p2) / np.log(4.0), 0.0, 1.0)
+    return alpha * p2max / p2 * high ** w_hi * low ** w_lo
 
 
-def family_table(alpha, high, p2min, p2max, n=TABLE_N):
+def family_table(alpha, high, p2min, p2max, n=TABLE_N, low=1.0):
     lo, hi = np.log(p2min) - 1e-3, np.log(p2max) + 1e-3
     p2 = np.exp(np.linspace(lo, hi, n))
-    return np.log(family_mult(alpha, high, p2, p2min, p2max)).astype(np.float32), lo, hi
+    return np.log(family_mult(alpha, high, p2, p2min, p2max, low)).astype(np.float32), lo, hi
+
+
+def survey(ctx, L, seeds, members, therm=100, transform_seed=5, max_iter=5000):
+    """Fixed multipliers family_mult(alpha, high, low) over configurations:
+    {member: [(steps, fallbacks, cost), ...]} with cost = steps + 11 x
+    fallbacks; a member that does not converge in max_iter steps costs 99999."""
+    res = {m: [] for m in members}
+    for beta, Uh in hmc_configs(ctx, L, [6.0] * len(seeds), seeds, therm, 1, 0):
+        for m in members:
+            U = prepared_links(ctx, Uh, transform_seed)
+            fa = LandauFA(U)
+            p2min, p2max = fa.p2range()
+            fa.set_table(*family_table(m[0], m[1], p2min, p2max, low=m[2]))
+            g = Lattice(ctx, 3, F64, U.grid).set_unit()
+            it, fb, th = fa.run(g, tol=1e-12, max_iter=max_iter)
+            res[m].append((it, fb, it + 11 * fb) if th < 1e-12 else (it, fb, 99999))
+            fa.close()
+    return res
 
 
 def collect(ctx, U, beta, tol=1e-12, nbins=24, max_steps=400, omega=1.7, or_sweeps=10, sample=None):
@@ -220,7 +241,7 @@ def load_weights(path=WEIGHTS):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["train", "compare"])
+    ap.add_argument("mode", choices=["train", "compare", "survey"])
     ap.add_argument("--configs", type=int, default=256)
     ap.add_argument("--chains", type=int, default=16)
     ap.add_argument("--L", type=int, default=24)
@@ -230,11 +251,20 @@ def main():
     ap.add_argument("--eval-configs", type=int, default=32)
     ap.add_argument("--eval-therm", type=int, default=200)
     ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--seed0", type=int, default=11, help="survey: HMC seed of the first configuration")
     ap.add_argument("--json", default=None)
     ap.add_argument("--sample-decades", type=int, default=0,
                     help="search this many random decades per configuration (0: every decade)")
     args = ap.parse_args()
     ctx = Context(0)
+    if args.mode == "survey":
+        members = [(a, h, b) for a in (0.06, 0.08, 0.1, 0.12) for h in (1.0, 0.6, 0.35) for b in (1.0, 2.0)]
+        seeds = list(range(args.seed0, args.seed0 + args.configs))
+        res = survey(ctx, args.L, seeds, members, therm=args.therm)
+        for c, m, v in sorted((float(np.mean([x[2] for x in v])), m, v) for m, v in res.items()):
+            print(json.dumps({"alpha": m[0], "high": m[1], "low": m[2], "mean_cost": c, "cost": [x[2] for x in v],
+                              "fallbacks": [x[1] for x in v]}))
+        return
     if args.mode == "train":
         t0 = time.time()
         rng = np.random.default_rng(99)
