@@ -257,6 +257,29 @@ template <class T> struct Group<SU3, T>
 			}
 		return r;
 	}
+	// c = a * b for special unitary a, b: rows 0 and 1 of the product (only
+	// rows 0 and 1 of a are read), row 2 rebuilt as conj(row 0 x row 1)
+	MESH_HD static E mul_r2(E const &a, E const &b)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 2; ++i)
+#pragma unroll
+			for (int j = 0; j < 3; ++j)
+			{
+				T re = 0, im = 0;
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+				{
+					re += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * j] - a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * j + 1];
+					im += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * j + 1] + a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * j];
+				}
+				r.v[6 * i + 2 * j] = re;
+				r.v[6 * i + 2 * j + 1] = im;
+			}
+		complete_row2(r);
+		return r;
+	}
 	// c = a * b^dagger:  c_ij = sum_k a_ik conj(b_jk)
 	MESH_HD static E mul_nd(E const &a, E const &b)
 	{
@@ -640,7 +663,7 @@ template <class T> struct Group<SU3, T>
 //   (cr, ci) += (ar, ai) * (br, br);  (cr, ci) += (-ai, ar) * (bi, bi),
 // halving the FMA instruction count of the 3x3 products.
 // ---------------------------------------------------------------------------
-struct Su3F2
+template <int FORM> struct Su3F2T
 {
 	using E = Group<SU3, float>::E;
 	__device__ __forceinline__ static unsigned long long pk(float a, float b)
@@ -661,56 +684,102 @@ struct Su3F2
 		return d;
 	}
 	// generic product with operand access functors: c_ij = sum_k A(i,k) B(k,j)
-	// where A(i,k) = (ar, ai) and B(k,j) = (br, bi)
-	template <class FA, class FB> __device__ __forceinline__ static E prod(FA fa, FB fb)
+	// for the rows i < NRW, where A(i,k) = (ar, ai) and B(k,j) = (br, bi).
+	// FORM 1: the pairs are (re, im) of A against broadcast parts of B:
+	//   (cr, ci) += (ar, ai) * (br, br) + (-ai, ar) * (bi, bi);
+	// FORM 2: broadcast parts of A against the (re, im) pairs of B:
+	//   (cr, ci) += (ar, ar) * (br, bi) + (ai, ai) * (-bi, br).
+	template <int NRW, class FA, class FB> __device__ __forceinline__ static E prod(FA fa, FB fb)
 	{
 		E r;
-#pragma unroll
-		for (int i = 0; i < 3; ++i)
+		if constexpr (FORM == 1)
 		{
-			unsigned long long an[3], ar[3];
 #pragma unroll
-			for (int k = 0; k < 3; ++k)
+			for (int i = 0; i < NRW; ++i)
 			{
-				float re, im;
-				fa(i, k, re, im);
-				an[k] = pk(re, im);
-				ar[k] = pk(-im, re);
-			}
-#pragma unroll
-			for (int j = 0; j < 3; ++j)
-			{
-				unsigned long long acc = 0ull;
+				unsigned long long an[3], ar[3];
 #pragma unroll
 				for (int k = 0; k < 3; ++k)
 				{
 					float re, im;
-					fb(k, j, re, im);
-					acc = fma2(an[k], pk(re, re), acc);
-					acc = fma2(ar[k], pk(im, im), acc);
+					fa(i, k, re, im);
+					an[k] = pk(re, im);
+					ar[k] = pk(-im, re);
 				}
-				upk(acc, r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+				{
+					unsigned long long acc = 0ull;
+#pragma unroll
+					for (int k = 0; k < 3; ++k)
+					{
+						float re, im;
+						fb(k, j, re, im);
+						acc = fma2(an[k], pk(re, re), acc);
+						acc = fma2(ar[k], pk(im, im), acc);
+					}
+					upk(acc, r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
+				}
+			}
+		}
+		else
+		{
+			unsigned long long bn[3][3], bs[3][3];
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+				{
+					float re, im;
+					fb(k, j, re, im);
+					bn[k][j] = pk(re, im);
+					bs[k][j] = pk(-im, re);
+				}
+#pragma unroll
+			for (int i = 0; i < NRW; ++i)
+			{
+				unsigned long long acc[3] = {0ull, 0ull, 0ull};
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+				{
+					float re, im;
+					fa(i, k, re, im);
+					unsigned long long rr = pk(re, re), ii = pk(im, im);
+#pragma unroll
+					for (int j = 0; j < 3; ++j)
+					{
+						acc[j] = fma2(rr, bn[k][j], acc[j]);
+						acc[j] = fma2(ii, bs[k][j], acc[j]);
+					}
+				}
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+					upk(acc[j], r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
 			}
 		}
 		return r;
 	}
-	__device__ __forceinline__ static E mul(E const &a, E const &b)
+	template <int NRW = 3> __device__ __forceinline__ static E mul(E const &a, E const &b)
 	{
-		return prod([&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
-		            [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
+		return prod<NRW>(
+		    [&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
+		    [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
 	}
 	// a b^dagger: B(k,j) = conj(b_jk)
 	__device__ __forceinline__ static E mul_nd(E const &a, E const &b)
 	{
-		return prod([&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
-		            [&](int k, int j, float &re, float &im) { re = b.v[6 * j + 2 * k]; im = -b.v[6 * j + 2 * k + 1]; });
+		return prod<3>(
+		    [&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
+		    [&](int k, int j, float &re, float &im) { re = b.v[6 * j + 2 * k]; im = -b.v[6 * j + 2 * k + 1]; });
 	}
 	// a^dagger b: A(i,k) = conj(a_ki)
 	__device__ __forceinline__ static E mul_dn(E const &a, E const &b)
 	{
-		return prod([&](int i, int k, float &re, float &im) { re = a.v[6 * k + 2 * i]; im = -a.v[6 * k + 2 * i + 1]; },
-		            [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
+		return prod<3>(
+		    [&](int i, int k, float &re, float &im) { re = a.v[6 * k + 2 * i]; im = -a.v[6 * k + 2 * i + 1]; },
+		    [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
 	}
 };
+using Su3F2 = Su3F2T<1>;
 
 } // namespace meshgb

@@ -273,6 +273,18 @@ template <int GRP, class T, int ND, bool ROWS = false> struct LinkLoad
 			Soa<T, Gp::NR>::template load<CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
 		return e;
 	}
+	// rows 0 and 1 only (row 2 left unset) where ROWS applies; else the link
+	__device__ __forceinline__ E rows(int mu, int64_t s) const
+	{
+		if constexpr (ROWS && GRP == SU3)
+		{
+			E e;
+			Soa<T, Gp::NR>::template load_head<12, CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
+			return e;
+		}
+		else
+			return (*this)(mu, s);
+	}
 };
 
 // rebuilt-row link loads for SU(3) in FP32 (the mixed-precision HMC links)
@@ -317,21 +329,44 @@ __global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restric
 	grid_sum<kBlock>(acc, out);
 }
 
-// 3x3 products of the force: packed FP32x2 FMAs for SU(3) float when F2
-template <int GRP, class T, bool F2> struct Prod
+// 3x3 products of the force: packed FP32x2 FMAs for SU(3) float when F2 > 0
+// (F2 = 1 or 2: the two pairings of Su3F2T). mul_r2: the product of two
+// special unitary matrices from rows 0 and 1 of the left one (row 2 of the
+// result rebuilt); the plain product for the other groups.
+template <int GRP, class T, int F2> struct Prod
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	__device__ __forceinline__ static E mul(E const &a, E const &b) { return Gp::mul(a, b); }
 	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return Gp::mul_nd(a, b); }
 	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return Gp::mul_dn(a, b); }
+	__device__ __forceinline__ static E mul_r2(E const &a, E const &b)
+	{
+		if constexpr (GRP == SU3)
+			return Gp::mul_r2(a, b);
+		else
+			return Gp::mul(a, b);
+	}
 };
-template <> struct Prod<SU3, float, true>
+template <int F2> struct ProdF2
 {
 	using E = Group<SU3, float>::E;
-	__device__ __forceinline__ static E mul(E const &a, E const &b) { return Su3F2::mul(a, b); }
-	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return Su3F2::mul_nd(a, b); }
-	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return Su3F2::mul_dn(a, b); }
+	using S = Su3F2T<F2>;
+	__device__ __forceinline__ static E mul(E const &a, E const &b) { return S::template mul<3>(a, b); }
+	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return S::mul_nd(a, b); }
+	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return S::mul_dn(a, b); }
+	__device__ __forceinline__ static E mul_r2(E const &a, E const &b)
+	{
+		E r = S::template mul<2>(a, b);
+		Group<SU3, float>::complete_row2(r);
+		return r;
+	}
+};
+template <> struct Prod<SU3, float, 1> : ProdF2<1>
+{
+};
+template <> struct Prod<SU3, float, 2> : ProdF2<2>
+{
 };
 
 // staple sum for link (x, mu) in the reference's association and summation
@@ -546,7 +581,7 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 // with the updated momentum (and project_on_group_fast when `reunit`), which
 // saves the separate link-update kernel's reads of U and P. The force of every
 // link reads U only, so writing Uout is race free.
-template <int GRP, class T, int ND, int NT, int MINB, bool F2 = false, bool ROWS = false, bool FUSE = false>
+template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
@@ -576,8 +611,18 @@ __global__ void __launch_bounds__(NT, MINB)
 			for (int q = 0; q < ND * (ND - 1) / 2; ++q)
 			{
 				int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
-				E ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-				E dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+				E ab, dc;
+				if constexpr (ROWS)
+				{
+					// special unitary links: products from rows 0, 1 of the left factor
+					ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+					dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+				}
+				else
+				{
+					ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+					dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+				}
 				E pl = Pr::mul_nd(ab, dc);
 				T xa[NA];
 				Gp::proj(pl, xa);
@@ -594,10 +639,13 @@ __global__ void __launch_bounds__(NT, MINB)
 					if (nu == mu)
 						continue;
 					int64_t y = eo_shift1<ND>(g, st, nu, -1);
-					E e = ld(mu, y);
 					E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
-					E h = ld(nu, y);
-					Gp::add_to(S, Pr::mul_dn(Pr::mul(e, f), h));
+					E ef;
+					if constexpr (ROWS)
+						ef = Pr::mul_r2(ld.rows(mu, y), f);
+					else
+						ef = Pr::mul(ld(mu, y), f);
+					Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
 				}
 				E W = Pr::mul(ld(mu, s), S);
 				T xa[NA];
@@ -1245,14 +1293,17 @@ template <int GRP, class T, int ND> struct Ops
 		int lt[4]; // log2 tile extents
 		int threads, minb;
 		char const *name;
-		bool f2 = false; // packed FP32x2 products (SU(3) float only)
+		int f2 = 0;        // packed FP32x2 products, pairing 1 or 2 (SU(3) float only)
+		bool full = false; // read all 18 reals of SU(3) FP32 links even where rows 0, 1 would do
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
 	// packed FP32x2 products; 14-17 and 21-22: thread per site
 	// (k_momentum_step_site) with FP32x2 products; 18-20: thread per site,
-	// plain products
-	static constexpr int kForceVariants = 23;
+	// plain products; 23-24: thread per site, FP32x2, whole links read (no
+	// row rebuilt: fewer products, more bytes through L1); 25-26: thread per
+	// site, FP32x2 with the second pairing (broadcast left factor)
+	static constexpr int kForceVariants = 27;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1279,7 +1330,11 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk"},
 		    {2, {1, 2, 2, 3}, 256, 2, "site/tile2x4x4x8/256thr/2blk"},
 		    {2, {2, 2, 2, 3}, 512, 1, "site/tile4x4x4x8/512thr/1blk/f32x2", true},
-		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2", true}};
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2", true},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/full", true, true},
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2/full", true, true},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2b", 2},
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1301,7 +1356,7 @@ template <int GRP, class T, int ND> struct Ops
 	static void launch_force(int v, Field &P, Field const &U, T coef, RedSlot kin, bool rows = false)
 	{
 		if constexpr (kRows<GRP, T>)
-			if (rows)
+			if (rows && !force_variant(v).full)
 				return launch_force_t<true>(v, P, U, coef, kin);
 		launch_force_t<false>(v, P, U, coef, kin);
 	}
@@ -1361,26 +1416,36 @@ template <int GRP, class T, int ND> struct Ops
 	{
 		if constexpr (ND == 4)
 		{
-			if (fv.f2)
+			if constexpr (kF2)
 			{
-				if constexpr (kF2)
-				{
-					if (fv.threads == 512)
-						k_momentum_step_site<GRP, T, 4, 512, 1, true, ROWS><<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin);
-					else if (fv.threads == 128 && fv.minb == 4)
-						k_momentum_step_site<GRP, T, 4, 128, 4, true, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
-					else if (fv.threads == 128)
-						k_momentum_step_site<GRP, T, 4, 128, 3, true, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
-					else
-						k_momentum_step_site<GRP, T, 4, 256, 2, true, ROWS><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
-				}
+				if (fv.f2 == 2)
+					return site_cfg<2, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
+				if (fv.f2 == 1)
+					return site_cfg<1, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
 			}
-			else if (fv.threads == 128 && fv.minb == 4)
-				k_momentum_step_site<GRP, T, 4, 128, 4, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
-			else if (fv.threads == 128)
-				k_momentum_step_site<GRP, T, 4, 128, 3, false, ROWS><<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin);
+			site_cfg<0, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
+		}
+	}
+	// the launch configurations of the thread-per-site kernel (pairing 2 only
+	// in the 128x4 and 512x1 configurations)
+	template <int F2, bool ROWS, bool FUSE>
+	static void site_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u, T *p,
+	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
+	{
+		if (fv.threads == 512)
+			k_momentum_step_site<GRP, T, 4, 512, 1, F2, ROWS, FUSE>
+			    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+		else if (F2 == 2 || (fv.threads == 128 && fv.minb == 4))
+			k_momentum_step_site<GRP, T, 4, 128, 4, F2, ROWS, FUSE>
+			    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+		else if constexpr (F2 != 2)
+		{
+			if (fv.threads == 128)
+				k_momentum_step_site<GRP, T, 4, 128, 3, F2, ROWS, FUSE>
+				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 			else
-				k_momentum_step_site<GRP, T, 4, 256, 2, false, ROWS><<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin);
+				k_momentum_step_site<GRP, T, 4, 256, 2, F2, ROWS, FUSE>
+				    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 		}
 	}
 	// tiles of variant fv over g and the grid size (at most minb blocks per SM)
@@ -1401,7 +1466,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
-	static constexpr int kMdFirst = 14, kMdLast = 22; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 26; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4 || sizeof(T) != 4)
@@ -1413,9 +1478,16 @@ template <int GRP, class T, int ND> struct Ops
 	}
 	static void launch_md(int v, Field &P, Field const &Uin, Field &Uout, T coef, T tu, int reunit, RedSlot kin)
 	{
+		if (force_variant(v).full)
+			launch_md_t<false>(v, P, Uin, Uout, coef, tu, reunit, kin);
+		else
+			launch_md_t<kRows<GRP, T>>(v, P, Uin, Uout, coef, tu, reunit, kin);
+	}
+	template <bool R>
+	static void launch_md_t(int v, Field &P, Field const &Uin, Field &Uout, T coef, T tu, int reunit, RedSlot kin)
+	{
 		if constexpr (ND == 4)
 		{
-			constexpr bool R = kRows<GRP, T>;
 			auto &c = *Uin.ctx;
 			Geom const &g = Uin.geom;
 			ForceVariant fv = force_variant(v);
@@ -1424,33 +1496,17 @@ template <int GRP, class T, int ND> struct Ops
 			T const *u = static_cast<T const *>(Uin.d);
 			T *p = static_cast<T *>(P.d);
 			T *uo = static_cast<T *>(Uout.d);
-			if (fv.f2)
+			if constexpr (kF2)
 			{
-				if constexpr (kF2)
-				{
-					if (fv.threads == 512)
-						k_momentum_step_site<GRP, T, 4, 512, 1, true, R, true>
-						    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-					else if (fv.threads == 128 && fv.minb == 4)
-						k_momentum_step_site<GRP, T, 4, 128, 4, true, R, true>
-						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-					else if (fv.threads == 128)
-						k_momentum_step_site<GRP, T, 4, 128, 3, true, R, true>
-						    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-					else
-						k_momentum_step_site<GRP, T, 4, 256, 2, true, R, true>
-						    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-				}
+				if (fv.f2 == 2)
+					site_cfg<2, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
+				else if (fv.f2 == 1)
+					site_cfg<1, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
+				else
+					site_cfg<0, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
 			}
-			else if (fv.threads == 128 && fv.minb == 4)
-				k_momentum_step_site<GRP, T, 4, 128, 4, false, R, true>
-				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-			else if (fv.threads == 128)
-				k_momentum_step_site<GRP, T, 4, 128, 3, false, R, true>
-				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 			else
-				k_momentum_step_site<GRP, T, 4, 256, 2, false, R, true>
-				    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				site_cfg<0, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
 			MESH_LAUNCH_CHECK();
 		}
 	}
