@@ -412,6 +412,33 @@ template <class T> struct Group<SU3, T>
 		r = csub(r, cmul(m.at(0, 1), csub(c, d)));
 		return cadd(r, cmul(m.at(0, 2), csub(e, f)));
 	}
+	// X^2 for antihermitian X: hermitian, (X^2)_ii = -sum_k |X_ik|^2 and
+	// (X^2)_ji = conj((X^2)_ij), so only the upper triangle is multiplied out
+	MESH_HD static E sq_ah(E const &X)
+	{
+		E r;
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+		{
+			T d = 0;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				d -= X.v[6 * i + 2 * k] * X.v[6 * i + 2 * k] + X.v[6 * i + 2 * k + 1] * X.v[6 * i + 2 * k + 1];
+			r.v[6 * i + 2 * i] = d;
+			r.v[6 * i + 2 * i + 1] = T(0);
+#pragma unroll
+			for (int j = i + 1; j < 3; ++j)
+			{
+				cx<T> z = {T(0), T(0)};
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+					z = cadd(z, cmul(X.at(i, k), X.at(k, j)));
+				r.set(i, j, z);
+				r.set(j, i, cconj(z));
+			}
+		}
+		return r;
+	}
 	// exp(X) for antihermitian traceless X with |X| < 1 (Frobenius norm), as
 	// the power series truncated after X^10 (remainder below |X|^11/11! =
 	// 2.5e-8) and reduced to a polynomial u0 + u1 X + u2 X^2 with the
@@ -466,7 +493,7 @@ template <class T> struct Group<SU3, T>
 		for (int k = 0; k < 8; ++k)
 			x[k] = o[k] * t;
 		E X = from_alg(x);
-		E X2 = mul(X, X);
+		E X2 = sq_ah(X);
 		// c1 = Tr(Q^2)/2 = |X|^2/2,  c0 = det(Q) = det(-iX) = -Im det(X)
 		T c1 = T(0.5) * kin(x);
 		T c0 = -det(X).im;

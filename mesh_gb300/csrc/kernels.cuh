@@ -273,6 +273,21 @@ template <int GRP, class T, int ND, bool ROWS = false> struct LinkLoad
 			Soa<T, Gp::NR>::template load<CACHE_KEEP>(U + int64_t(mu) * Gp::NR * V, V, s, e.v);
 		return e;
 	}
+	// prefetch of the planes a later load of link (mu, s) reads into L1
+	__device__ __forceinline__ void prefetch(int mu, int64_t s) const
+	{
+		if constexpr (sizeof(T) == 4)
+		{
+			constexpr int NP = (ROWS && GRP == SU3) ? 3 : (Gp::NR + 3) / 4;
+			T const *base = U + int64_t(mu) * Gp::NR * V;
+#pragma unroll
+			for (int k = 0; k < NP; ++k)
+			{
+				T const *p = k < Gp::NR / 4 ? base + (int64_t(k) * V + s) * 4 : base + int64_t(4 * (Gp::NR / 4)) * V + s * 2;
+				asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+			}
+		}
+	}
 	// rows 0 and 1 only (row 2 left unset) where ROWS applies; else the link
 	__device__ __forceinline__ E rows(int mu, int64_t s) const
 	{
@@ -581,7 +596,10 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 // with the updated momentum (and project_on_group_fast when `reunit`), which
 // saves the separate link-update kernel's reads of U and P. The force of every
 // link reads U only, so writing Uout is race free.
-template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false>
+//
+// PF: the links of the backward staples are prefetched into L1 when a site
+// starts, so that their L2 latency overlaps the forward loops.
+template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false, bool PF = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
@@ -606,6 +624,22 @@ __global__ void __launch_bounds__(NT, MINB)
 #pragma unroll
 				for (int a = 0; a < NA; ++a)
 					F[mu][a] = T(0);
+			if constexpr (PF)
+			{
+#pragma unroll 1
+				for (int nu = 0; nu < ND; ++nu)
+				{
+					int64_t y = eo_shift1<ND>(g, st, nu, -1);
+					ld.prefetch(nu, y);
+#pragma unroll 1
+					for (int mu = 0; mu < ND; ++mu)
+						if (mu != nu)
+						{
+							ld.prefetch(mu, y);
+							ld.prefetch(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
+						}
+				}
+			}
 			// forward plaquette loops, one per plane
 #pragma unroll 1
 			for (int q = 0; q < ND * (ND - 1) / 2; ++q)
@@ -690,7 +724,11 @@ __global__ void __launch_bounds__(NT, MINB)
 						p[a] -= coef * f[a];
 					Pv.template store<CACHE_STREAM>(s, p);
 					acc += double(Gp::kin(p));
-					E r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
+					E r;
+					if constexpr (ROWS)
+						r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
+					else
+						r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
 					if (reunit)
 						r = Gp::reunit_fast(r);
 					comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
@@ -1295,6 +1333,7 @@ template <int GRP, class T, int ND> struct Ops
 		char const *name;
 		int f2 = 0;        // packed FP32x2 products, pairing 1 or 2 (SU(3) float only)
 		bool full = false; // read all 18 reals of SU(3) FP32 links even where rows 0, 1 would do
+		bool pf = false;   // prefetch the backward-staple links (thread per site)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1302,8 +1341,9 @@ template <int GRP, class T, int ND> struct Ops
 	// (k_momentum_step_site) with FP32x2 products; 18-20: thread per site,
 	// plain products; 23-24: thread per site, FP32x2, whole links read (no
 	// row rebuilt: fewer products, more bytes through L1); 25-26: thread per
-	// site, FP32x2 with the second pairing (broadcast left factor)
-	static constexpr int kForceVariants = 27;
+	// site, FP32x2 with the second pairing (broadcast left factor); 27-28:
+	// thread per site, FP32x2, backward-staple links prefetched into L1
+	static constexpr int kForceVariants = 29;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1334,7 +1374,9 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/full", true, true},
 		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2/full", true, true},
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2b", 2},
-		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2}};
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/pf", 1, false, true},
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2/pf", 1, false, true}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1432,6 +1474,17 @@ template <int GRP, class T, int ND> struct Ops
 	static void site_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u, T *p,
 	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
 	{
+		if constexpr (F2 == 1)
+			if (fv.pf)
+			{
+				if (fv.threads == 512)
+					k_momentum_step_site<GRP, T, 4, 512, 1, F2, ROWS, FUSE, true>
+					    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				else
+					k_momentum_step_site<GRP, T, 4, 128, 4, F2, ROWS, FUSE, true>
+					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				return;
+			}
 		if (fv.threads == 512)
 			k_momentum_step_site<GRP, T, 4, 512, 1, F2, ROWS, FUSE>
 			    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
@@ -1466,7 +1519,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
-	static constexpr int kMdFirst = 14, kMdLast = 26; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 28; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4 || sizeof(T) != 4)
