@@ -53,10 +53,16 @@ def parse():
                          "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
                          "(plain and learned multiplier)")
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
+    ap.add_argument("--fp64", action="store_true",
+                    help="hmc workload: the plain all-FP64 chain (links, momenta, force in FP64) instead of the "
+                         "mixed-precision one, for the FP64-vs-mixed comparison")
     a = ap.parse_args()
     if a.lattice != 32:
         WORKLOAD["dims"] = [a.lattice] * 4
         WORKLOAD["name"] = WORKLOAD["name"].replace("32^4", f"{a.lattice}^4")
+    if a.fp64:
+        WORKLOAD["name"] = WORKLOAD["name"].replace("_mixed", "_fp64")
+    WORKLOAD["prec_bytes"] = 8 if a.fp64 else 4
     return a
 
 
@@ -75,10 +81,10 @@ def deltas_counts(n):
     return n_u, n - n_u
 
 
-def algorithmic_bytes_per_traj(dims, n):
+def algorithmic_bytes_per_traj(dims, n, prec_bytes=4):
     """Compulsory HBM bytes of one trajectory, every object read/written once:
     n_P (|U| + 2|P|) + n_U (2|U| + |P|) + |P| + 2(|U| + |P|) + 2|U|."""
-    _, U, P = sizes(dims)
+    _, U, P = sizes(dims, prec_bytes)
     n_u, n_p = deltas_counts(n)
     return n_p * (U + 2 * P) + n_u * (2 * U + P) + P + 2 * (U + P) + 2 * U
 
@@ -236,7 +242,8 @@ def run_ours(args):
     # refresh, the first link update, n_p momentum steps each fused with the
     # link update after it, plaquette, metropolis, accept copy
     launches_per_traj = 1 + 1 + n_p + 1 + 2
-    h = mg.Hmc(ctx, WORKLOAD["group"], mg.F32, grid, seed=WORKLOAD["seed"] + rank)
+    pb = WORKLOAD["prec_bytes"]
+    h = mg.Hmc(ctx, WORKLOAD["group"], mg.F64 if pb == 8 else mg.F32, grid, seed=WORKLOAD["seed"] + rank)
     h.randomize_gauge_field()
     h.run(beta, d, args.therm, use_graph=True)
     h.run(beta, d, args.warmup, use_graph=True)
@@ -273,7 +280,7 @@ def run_ours(args):
     # with CUDA events on the launching stream; du = 0 leaves U unchanged.
     # Algorithmic bytes per launch: one momentum step (|U| + 2|P|) and one
     # link update (2|U| + |P|)
-    _, Ub, Pb = sizes(dims)
+    _, Ub, Pb = sizes(dims, pb)
     B_f = Ub + 2 * Pb
     B_md = B_f + 2 * Ub + Pb
     U, P = h.U, h.P
@@ -309,10 +316,11 @@ def run_ours(args):
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "vs_baseline": None, "dtype": "f64" if pb == 8 else "f32", "data": "synthetic",
            "config": {"workload": WORKLOAD["name"], "lattice": dims, "beta": beta,
                       "integrator": f"{WORKLOAD['scheme']} eps={WORKLOAD['eps']} n={WORKLOAD['substeps']}",
-                      "precision": "FP32 links/momenta/force, FP64 sums/dH/Metropolis",
+                      "precision": "FP64 throughout" if pb == 8 else
+                                   "FP32 links/momenta/force, FP64 sums/dH/Metropolis",
                       "thermalisation": f"{args.therm} trajectories from a hot start, seed {WORKLOAD['seed']}",
                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                       "l2": "inputs larger than L2 (links 302 MB + momenta 134 MB > 129 MB)",
@@ -322,7 +330,9 @@ def run_ours(args):
                         "frac": achieved / peak, "traffic": ncu_traffic(),
                         "kernel": "k_momentum_step_site<SU3,float,4,..,f32x2,rows01,fused> (staples + force + "
                                   "momentum update + the following link update, one thread per site; links read "
-                                  "as rows 0,1, row 2 rebuilt)",
+                                  "as rows 0,1, row 2 rebuilt)" if pb == 4 else
+                                  "k_momentum_step_tiled<SU3,double> + k_evolve<SU3,double> (FP64: momentum step "
+                                  "and link update as two kernels)",
                         "algorithmic_bytes_per_launch": B_md, "avg_launch_ms": t_md * 1e3,
                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                         else "fallback 6.8 TB/s"},
@@ -330,8 +340,8 @@ def run_ours(args):
                        "momentum_step_alone_GBps": B_f / t_force / 1e9,
                        "link_update_ms": t_evolve * 1e3,
                        "link_update_GBps": (2 * Ub + Pb) / t_evolve / 1e9,
-                       "trajectory_algorithmic_GB": algorithmic_bytes_per_traj(dims, n) / 1e9,
-                       "trajectory_effective_GBps": algorithmic_bytes_per_traj(dims, n) / (ms / args.steps / 1e3)
+                       "trajectory_algorithmic_GB": algorithmic_bytes_per_traj(dims, n, pb) / 1e9,
+                       "trajectory_effective_GBps": algorithmic_bytes_per_traj(dims, n, pb) / (ms / args.steps / 1e3)
                        / 1e9},
            "clocks": clk, "gpu_launches": launches_per_traj * args.steps,
            "autotune": mg.tune_report().strip().splitlines()}
@@ -340,7 +350,8 @@ def run_ours(args):
     # reference's host layout is imported, one trajectory runs, the field is
     # exported back (pinned host memory), every step
     if not args.no_e2e:
-        host_t = torch.empty((len(dims), grid.size, 18), dtype=torch.float32, pin_memory=True)
+        host_t = torch.empty((len(dims), grid.size, 18), dtype=torch.float64 if pb == 8 else torch.float32,
+                             pin_memory=True)
         host = host_t.numpy()
         host[...] = U.export()
         k_e2e = max(3, min(args.steps, 10))
@@ -354,7 +365,7 @@ def run_ours(args):
                       "d2h_bytes_per_step": host.nbytes + 40, "steps": k_e2e,
                       "api": "mesh_hmc_run_host (import U, one trajectory, export U)"}
 
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and pb == 4:
         Uh = U.export()
         Ph = P.export()
         v, cores, tf, te, tp = cpu_baseline_md(Uh, Ph, dims, n, beta, float(d[1]))

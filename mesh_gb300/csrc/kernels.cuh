@@ -706,139 +706,6 @@ __global__ void __launch_bounds__(NT, MINB)
 		grid_sum<NT>(acc, kin);
 }
 
-// The thread-per-site momentum step (4D) split over two lanes per site: lane
-// h = 0 owns the directions 0, 1 and the planes (0,1), (0,2), (0,3); lane
-// h = 1 owns 2, 3 and the planes (2,3), (1,2), (1,3). Each lane closes its
-// planes' forward loops, keeps +-proj for its own directions and hands the
-// other lane its share with a shuffle (planes (0,2), (0,3): -X to lane 1's
-// directions 2, 3; planes (1,2), (1,3): +X to lane 0's direction 1); then it
-// sums the backward staples of its own two directions. Both lanes do 23 SU(3)
-// products and hold half the force accumulators, so the kernel runs with
-// more resident warps than k_momentum_step_site. Directions and signs are
-// selected arithmetically: the two lanes of a pair never diverge.
-template <int GRP, class T, int NT, int MINB, int F2, bool ROWS, bool FUSE>
-__global__ void __launch_bounds__(NT, MINB)
-    k_momentum_step_pair(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
-                         T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
-{
-	constexpr int ND = 4;
-	using Gp = Group<GRP, T>;
-	using E = typename Gp::E;
-	using Pr = Prod<GRP, T, F2>;
-	constexpr int NA = Gp::NA;
-	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
-	int const h = threadIdx.x & 1;
-	double acc = 0.0;
-	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
-	{
-		for (int t = threadIdx.x >> 1; t < ts.sites; t += NT / 2)
-		{
-			int x[ND];
-			tile_site<ND>(ts, tile, t, x);
-			Site<ND> st = site_from_coords<ND>(g, x);
-			int64_t s = eo_of<ND>(g, st);
-			T F0[NA], F1[NA]; // directions 2h and 2h + 1
-#pragma unroll
-			for (int a = 0; a < NA; ++a)
-				F0[a] = F1[a] = T(0);
-#pragma unroll 1
-			for (int q = 0; q < 3; ++q)
-			{
-				// lane 0: (0,1), (0,2), (0,3); lane 1: (2,3), (1,2), (1,3)
-				int mu = h == 0 ? 0 : (q == 0 ? 2 : 1);
-				int nu = h == 0 ? q + 1 : (q == 0 ? 3 : q + 1);
-				E ab, dc;
-				if constexpr (ROWS)
-				{
-					ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-					dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
-				}
-				else
-				{
-					ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-					dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
-				}
-				T xa[NA];
-				Gp::proj(Pr::mul_nd(ab, dc), xa);
-				// own share: +X on mu, -X on nu where the lane owns them
-				T own0 = (q == 0 || h == 0) ? T(1) : T(-1); // F0: mu (lane 0) / nu = 2 (lane 1, q = 1)
-				T own1 = q == 0 ? T(-1) : (h == 1 && q == 2 ? T(-1) : T(0));
-				if (h == 1 && q == 2)
-					own0 = T(0); // lane 1, plane (1,3): its own direction is 3 (F1)
-				// the partner's share, sent with its sign: lane 0 sends -X
-				// (for lane 1's direction nu), lane 1 sends +X (for lane 0's
-				// direction 1); received into F0 (lane 1, q = 1: direction 2) or
-				// F1 (lane 0: direction 1; lane 1, q = 2: direction 3)
-				T send = h == 0 ? T(-1) : T(1);
-				T in0 = (q != 0 && h == 1 && q == 1) ? T(1) : T(0);
-				T in1 = (q != 0 && !(h == 1 && q == 1)) ? T(1) : T(0);
-#pragma unroll
-				for (int a = 0; a < NA; ++a)
-				{
-					T r = __shfl_xor_sync(0xffffffffu, send * xa[a], 1);
-					F0[a] += own0 * xa[a] + in0 * r;
-					F1[a] += own1 * xa[a] + in1 * r;
-				}
-			}
-			// backward staples of the lane's two directions
-#pragma unroll 1
-			for (int l = 0; l < 2; ++l)
-			{
-				int mu = 2 * h + l;
-				E S = Gp::zero();
-#pragma unroll 1
-				for (int nu = 0; nu < ND; ++nu)
-				{
-					if (nu == mu)
-						continue;
-					int64_t y = eo_shift1<ND>(g, st, nu, -1);
-					E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
-					E ef;
-					if constexpr (ROWS)
-						ef = Pr::mul_r2(ld.rows(mu, y), f);
-					else
-						ef = Pr::mul(ld(mu, y), f);
-					Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
-				}
-				T xa[NA];
-				Gp::proj(Pr::mul(ld(mu, s), S), xa);
-#pragma unroll
-				for (int a = 0; a < NA; ++a)
-				{
-					F0[a] += l == 0 ? xa[a] : T(0);
-					F1[a] += l == 1 ? xa[a] : T(0);
-				}
-			}
-#pragma unroll 1
-			for (int l = 0; l < 2; ++l)
-			{
-				int mu = 2 * h + l;
-				auto Pv = comp<T, NA>(P, g.V, mu);
-				T p[NA];
-				Pv.template load<CACHE_STREAM>(s, p);
-#pragma unroll
-				for (int a = 0; a < NA; ++a)
-					p[a] -= coef * (l == 0 ? F0[a] : F1[a]);
-				Pv.template store<CACHE_STREAM>(s, p);
-				acc += double(Gp::kin(p));
-				if constexpr (FUSE)
-				{
-					E r;
-					if constexpr (ROWS)
-						r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
-					else
-						r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
-					if (reunit)
-						r = Gp::reunit_fast(r);
-					comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
-				}
-			}
-		}
-	}
-	if (kin.result)
-		grid_sum<NT>(acc, kin);
-}
-
 template <int GRP, class T, int ND>
 __global__ void __launch_bounds__(kBlock) k_staple_sum(Geom g, int mu, T const *__restrict__ U, T *__restrict__ S)
 {
@@ -1439,9 +1306,8 @@ template <int GRP, class T, int ND> struct Ops
 	// (k_momentum_step_site) with FP32x2 products; 18-20: thread per site,
 	// plain products; 23-24: thread per site, FP32x2, whole links read (no
 	// row rebuilt: fewer products, more bytes through L1); 25-26: thread per
-	// site, FP32x2 with the second pairing (broadcast left factor); 27-30: two
-	// lanes per site (k_momentum_step_pair), FP32x2, SU(3) FP32 only
-	static constexpr int kForceVariants = 31;
+	// site, FP32x2 with the second pairing (broadcast left factor)
+	static constexpr int kForceVariants = 27;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1472,11 +1338,7 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/full", true, true},
 		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2/full", true, true},
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2b", 2},
-		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2},
-		    {3, {1, 1, 2, 3}, 256, 2, "pair/tile2x2x4x8/256thr/2blk/f32x2", 1},
-		    {3, {1, 1, 2, 3}, 256, 3, "pair/tile2x2x4x8/256thr/3blk/f32x2", 1},
-		    {3, {1, 1, 1, 3}, 128, 5, "pair/tile2x2x2x8/128thr/5blk/f32x2", 1},
-		    {3, {1, 1, 1, 3}, 128, 6, "pair/tile2x2x2x8/128thr/6blk/f32x2", 1}};
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1484,7 +1346,7 @@ template <int GRP, class T, int ND> struct Ops
 		if (v < 0 || v >= n_force_variants())
 			return false;
 		ForceVariant fv = force_variant(v);
-		if ((fv.f2 || fv.tiled == 3) && !kF2)
+		if (fv.f2 && !kF2)
 			return false;
 		if (!fv.tiled)
 			return true;
@@ -1524,9 +1386,7 @@ template <int GRP, class T, int ND> struct Ops
 		{
 			unsigned b = 0;
 			TileSpec ts = tiles_for(g, fv, c, b);
-			if (fv.tiled == 3)
-				pair_cfg<ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
-			else if (fv.tiled == 2)
+			if (fv.tiled == 2)
 				launch_force_site<ROWS>(fv, b, g, ts, u, p, coef, kin, c);
 			else if (fv.f2)
 			{
@@ -1570,27 +1430,6 @@ template <int GRP, class T, int ND> struct Ops
 			site_cfg<0, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
 		}
 	}
-	// the launch configurations of the two-lane kernel (SU(3) FP32 only)
-	template <bool ROWS, bool FUSE>
-	static void pair_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u, T *p,
-	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
-	{
-		if constexpr (kF2)
-		{
-			if (fv.threads == 256 && fv.minb == 2)
-				k_momentum_step_pair<GRP, T, 256, 2, 1, ROWS, FUSE>
-				    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-			else if (fv.threads == 256)
-				k_momentum_step_pair<GRP, T, 256, 3, 1, ROWS, FUSE>
-				    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-			else if (fv.minb == 5)
-				k_momentum_step_pair<GRP, T, 128, 5, 1, ROWS, FUSE>
-				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-			else
-				k_momentum_step_pair<GRP, T, 128, 6, 1, ROWS, FUSE>
-				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-		}
-	}
 	// the launch configurations of the thread-per-site kernel (pairing 2 only
 	// in the 128x4 and 512x1 configurations)
 	template <int F2, bool ROWS, bool FUSE>
@@ -1631,7 +1470,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
-	static constexpr int kMdFirst = 14, kMdLast = 30; // the thread-per-site and two-lane variants
+	static constexpr int kMdFirst = 14, kMdLast = 26; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4 || sizeof(T) != 4)
@@ -1663,9 +1502,7 @@ template <int GRP, class T, int ND> struct Ops
 			T *uo = static_cast<T *>(Uout.d);
 			if constexpr (kF2)
 			{
-				if (fv.tiled == 3)
-					pair_cfg<R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
-				else if (fv.f2 == 2)
+				if (fv.f2 == 2)
 					site_cfg<2, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
 				else if (fv.f2 == 1)
 					site_cfg<1, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
