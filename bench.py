@@ -48,10 +48,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattice", type=int, default=32,
                     help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
-    ap.add_argument("--workload", choices=["hmc", "batch", "landau"], default="hmc",
+    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson"], default="hmc",
                     help="hmc: the headline line; batch: 64 SU(2) replicas in one persistent launch against 64 "
                          "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
-                         "(plain and learned multiplier)")
+                         "(plain and learned multiplier); wilson: all r x t Wilson loops of a thermalised "
+                         "configuration")
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
     ap.add_argument("--fp64", action="store_true",
                     help="hmc workload: the plain all-FP64 chain (links, momenta, force in FP64) instead of the "
@@ -462,6 +463,43 @@ def run_batch(args):
     return 0
 
 
+def run_wilson(args):
+    """All rectangular Wilson loops W(r, t), r = 1..L/2, t = 1..L, of a
+    thermalised SU(3) L^4 beta = 6.0 configuration (mixed-precision HMC,
+    hot start, seed 7), FP32 links: loop sets per second and the effective
+    bandwidth (every line extension reads two link objects and writes one per
+    site, every loop sum reads the three spatial lines and the temporal line:
+    four per site)."""
+    import numpy as np
+    import torch
+
+    import mesh_gb300 as mg
+
+    torch.cuda.set_device(0)
+    ctx = mg.Context(0)
+    L = args.lattice
+    h = mg.Hmc(ctx, 3, mg.F32, mg.Grid([L] * 4), seed=7)
+    h.randomize_gauge_field()
+    h.run(6.0, mg.make_deltas("2mn", 0.5, 20), args.therm, use_graph=True)
+    R, T = L // 2, L
+    W = mg.wilson_loops(h.U, R, T)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        W = mg.wilson_loops(h.U, R, T)
+    dt = (time.perf_counter() - t0) / args.steps
+    V = L ** 4
+    set_bytes = 72 * V * (3 * ((T - 1) + 3 * (R - 1)) + 4 * R * T)
+    out = {"metric": "SU(3) Wilson loop sets/s", "value": 1.0 / dt, "unit": "sets/s", "n_gpus": 1,
+           "steps": args.steps, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"su3_wilson_loops_{L}^4_r1..{R}_t1..{T}", "thermalisation": f"{args.therm} "
+                      "trajectories, seed 7", "launches_per_set": (T - 1) + 3 * (R - 1) + R * T},
+           "seconds_per_set": dt, "effective_GBps": set_bytes / dt / 1e9,
+           "W": {f"{r + 1}x{t + 1}": float(W[r, t]) for r in range(min(R, 4)) for t in range(min(T, 4))}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_landau(args):
     """Time to theta < 1e-12 from a Haar-random gauge transform of thermalised
     SU(3) L^4 beta = 6.0 configurations: FP64 overrelaxation (omega 1.7) and
@@ -507,6 +545,8 @@ def main():
         return run_batch(args)
     if args.workload == "landau":
         return run_landau(args)
+    if args.workload == "wilson":
+        return run_wilson(args)
     return run_ours(args)
 
 

@@ -29,6 +29,7 @@
 #include <stdexcept>
 #include <string>
 #include <string_view>
+#include <tuple>
 #include <vector>
 
 namespace mesh {
@@ -279,6 +280,21 @@ template <class G> double wilsonAction(GaugeField<G> const &U, double beta)
 	double s = 0;
 	check(mesh_wilson_action(U.get(), beta, &s));
 	return s;
+}
+// wilson(const Mesh<G>&, int maxN) of src/old/mesh/wilson.cpp:40-75: the
+// rectangular loops (n, t, W) for n = 1..maxN, t = 1..maxT (default: L3)
+template <class G>
+std::vector<std::tuple<int, int, double>> wilson(GaugeField<G> const &U, int maxN, int maxT = -1)
+{
+	if (maxT < 0)
+		maxT = U.grid().shape(3);
+	std::vector<double> w(size_t(maxN) * size_t(maxT));
+	check(mesh_wilson_loops(U.get(), maxN, maxT, w.data()));
+	std::vector<std::tuple<int, int, double>> r;
+	for (int n = 1; n <= maxN; ++n)
+		for (int t = 1; t <= maxT; ++t)
+			r.emplace_back(n, t, w[size_t(n - 1) * maxT + (t - 1)]);
+	return r;
 }
 template <class G> Lattice<G> stapleSum(GaugeField<G> const &U, int mu)
 {

@@ -153,6 +153,14 @@ int mesh_field_norm2(mesh_field a, double *out);
 int mesh_plaquette(mesh_field U, double *out);
 /* Wilson action (1 - plaquette) * beta * Nd(Nd-1)/2 * V (utils.h:141-146) */
 int mesh_wilson_action(mesh_field U, double beta, double *out);
+/* Rectangular Wilson loops W(r, t) for r = 1..max_r, t = 1..max_t in the planes
+ * (mu, 3), mu = 0, 1, 2: the legacy wilson() of src/old/mesh/wilson.cpp:40-75
+ * (spatial line of r links, temporal line of t links, averaged over sites and
+ * the three spatial directions), normalised like the plaquette (ReTr / Nc, so
+ * W(1, 1) is the mean plaquette of the planes (mu, 3)). out[(r-1) max_t + t-1].
+ * 4D lattices; max_r <= min(L0, L1, L2), max_t <= L3. Allocates (max_t + 3)
+ * link components of scratch for the call. */
+int mesh_wilson_loops(mesh_field U, int max_r, int max_t, double *out);
 
 /* Plaquette without any device allocation. No counterpart in the reference.
  * For callers that cannot call cudaMalloc when they measure: applications

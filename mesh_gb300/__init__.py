@@ -90,6 +90,7 @@ SIGNATURES = {
     "mesh_field_norm2": (_I, [_P, _DP]),
     "mesh_plaquette": (_I, [_P, _DP]),
     "mesh_wilson_action": (_I, [_P, _D, _DP]),
+    "mesh_wilson_loops": (_I, [_P, _I, _I, _DP]),
     "mesh_plaquette_noalloc": (_I, [_I, _I, _I, _I, _I32P, _P, _P, _DP]),
     "mesh_staple_sum": (_I, [_P, _P, _I]),
     "mesh_wilson_deriv": (_I, [_P, _P, _I, _D]),
@@ -409,6 +410,15 @@ def wilson_action(U: Field, beta: float) -> float:
     out = C.c_double()
     _chk(load().mesh_wilson_action(U.h, beta, C.byref(out)))
     return out.value
+
+
+def wilson_loops(U: Field, max_r: int, max_t: int) -> np.ndarray:
+    """Rectangular Wilson loops W(r, t) (r = 1..max_r spatial, t = 1..max_t
+    in direction 3), ReTr / Nc averaged over sites and the three spatial
+    directions: array [max_r, max_t]"""
+    out = np.zeros((max_r, max_t), dtype=np.float64)
+    _chk(load().mesh_wilson_loops(U.h, max_r, max_t, out.ctypes.data_as(_DP)))
+    return out
 
 
 def staple_sum(S: Field, U: Field, mu: int) -> Field:

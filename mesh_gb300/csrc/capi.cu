@@ -635,6 +635,62 @@ int mesh_plaquette(mesh_field Uh, double *out)
 	});
 }
 
+int mesh_wilson_loops(mesh_field Uh, int max_r, int max_t, double *out)
+{
+	return api([&] {
+		Field &U = F(Uh);
+		check_gauge(U);
+		require(out != nullptr, "null output");
+		require(U.nd == 4, "Wilson loops need a 4D lattice");
+		int lmin = std::min(U.dims[0], std::min(U.dims[1], U.dims[2]));
+		require(max_r >= 1 && max_r <= lmin, "max_r must be in 1..min(L0, L1, L2)");
+		require(max_t >= 1 && max_t <= U.dims[3], "max_t must be in 1..L3");
+		DeviceGuard dg(U.ctx->device);
+		Context &c = *U.ctx;
+		auto const &ops = ops_for(U);
+		size_t comp = size_t(U.geom.V) * size_t(U.nr) * U.real_bytes;
+		size_t nres = size_t(max_r) * size_t(max_t);
+		char *lines = nullptr; // max_t temporal lines, then the three spatial lines
+		double *res = nullptr;
+		MESH_CUDA(cudaMallocAsync(&lines, comp * size_t(max_t + 3), c.stream));
+		MESH_CUDA(cudaMallocAsync(&res, nres * sizeof(double), c.stream));
+		auto release = [&] {
+			cudaFreeAsync(lines, c.stream);
+			cudaFreeAsync(res, c.stream);
+		};
+		try
+		{
+			char *T1 = lines, *S = lines + comp * size_t(max_t);
+			char const *u = static_cast<char const *>(U.d);
+			MESH_CUDA(cudaMemcpyAsync(T1, u + 3 * comp, comp, cudaMemcpyDeviceToDevice, c.stream));
+			for (int t = 2; t <= max_t; ++t)
+				ops.line_extend(U, 3, t, T1 + comp * size_t(t - 2), T1 + comp * size_t(t - 1));
+			MESH_CUDA(cudaMemcpyAsync(S, u, 3 * comp, cudaMemcpyDeviceToDevice, c.stream));
+			RedSlot base = slot(c, SLOT_TMP);
+			for (int r = 1; r <= max_r; ++r)
+			{
+				if (r > 1)
+					for (int mu = 0; mu < 3; ++mu)
+						ops.line_extend(U, mu, r, S + comp * mu, S + comp * mu);
+				for (int t = 1; t <= max_t; ++t)
+					ops.wilson_rt(U, r, t, S, T1 + comp * size_t(t - 1),
+					              RedSlot{base.partials, res + size_t(r - 1) * max_t + (t - 1), base.counter});
+			}
+			MESH_CUDA(cudaMemcpyAsync(out, res, nres * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+			MESH_CUDA(cudaStreamSynchronize(c.stream));
+		}
+		catch (...)
+		{
+			release();
+			throw;
+		}
+		release();
+		double norm = 3.0 * double(U.geom.V) * double(group_nc(U.group));
+		for (size_t k = 0; k < nres; ++k)
+			out[k] /= norm;
+	});
+}
+
 int mesh_wilson_action(mesh_field Uh, double beta, double *out)
 {
 	return api([&] {

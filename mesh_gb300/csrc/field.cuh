@@ -119,6 +119,9 @@ struct OpsTable
 	// (then the two steps run separately)
 	bool (*hmc_md_step)(Field &P, Field const &Uin, Field &Uout, double coef, double tu, bool reunit, RedSlot *kin);
 	void (*hmc_tune_md)(Field &P, Field const &Uin, Field &Uout);
+	// Wilson loops (4D): Lout = Lprev U_dir(x + (n-1) dir); sum of the r x t loops
+	void (*line_extend)(Field const &U, int dir, int n, void const *Lprev, void *Lout);
+	void (*wilson_rt)(Field const &U, int r, int t, void const *S, void const *Tt, RedSlot out);
 };
 
 // autotuning registry (tune.cu): variant index per kernel/lattice key

@@ -706,6 +706,71 @@ __global__ void __launch_bounds__(NT, MINB)
 		grid_sum<NT>(acc, kin);
 }
 
+// ---------------------------------------------------------------------------
+// Wilson loops (legacy src/old/mesh/wilson.cpp:40-75): straight lines of links
+// built one link at a time, then the rectangular loops from four lines
+// ---------------------------------------------------------------------------
+// even/odd index of x + off e_dir for 0 <= off < L_dir (extents are even, so
+// the parity changes with off whether or not the step wraps)
+template <int ND> __device__ __forceinline__ int64_t eo_offset(Geom const &g, Site<ND> const &st, int dir, int off)
+{
+	int L = g.Ld(dir);
+	int32_t lex = st.lex + (st.x(dir) + off >= L ? off - L : off) * g.Sd(dir);
+	return int64_t(st.par ^ (off & 1)) * g.Vh + (lex >> 1);
+}
+
+// Lout(x) = Lprev(x) U_dir(x + (n - 1) dir): the line of n links from x
+// (Lout may be Lprev: every site reads and writes only its own line)
+template <int GRP, class T, int ND>
+__global__ void __launch_bounds__(kBlock)
+    k_line_extend(Geom g, int dir, int n, T const *Lprev, T const *__restrict__ U, T *Lout)
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	int off = (n - 1) % g.Ld(dir);
+	MESH_GRID_LOOP(s, g.V)
+	{
+		Site<ND> st = site_from_eo<ND>(g, s);
+		E a, b;
+		Soa<T, Gp::NR>::load(Lprev, g.V, s, a.v);
+		Soa<T, Gp::NR>::load(U + int64_t(dir) * Gp::NR * g.V, g.V, eo_offset<ND>(g, st, dir, off), b.v);
+		E c = Gp::mul(a, b);
+		Soa<T, Gp::NR>::store(Lout, g.V, s, c.v);
+	}
+}
+
+// sum over sites and mu < 3 of ReTr(S_mu(x) T(x + r mu) S_mu(x + t 3)^+ T(x)^+),
+// S: the three spatial lines of r links (components 0..2), T: the line of t
+// links in direction 3
+template <int GRP, class T, int ND>
+__global__ void __launch_bounds__(kBlock)
+    k_wilson_rt(Geom g, int r, int t, T const *__restrict__ S, T const *__restrict__ Tt, RedSlot out)
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	double acc = 0.0;
+	MESH_GRID_LOOP(s, g.V)
+	{
+		Site<ND> st = site_from_eo<ND>(g, s);
+		E d;
+		Soa<T, Gp::NR>::load(Tt, g.V, s, d.v);
+		int64_t xt = eo_offset<ND>(g, st, 3, t % g.Ld(3));
+		T sum = T(0);
+#pragma unroll 1
+		for (int mu = 0; mu < 3; ++mu)
+		{
+			T const *Smu = S + int64_t(mu) * Gp::NR * g.V;
+			E a, b, c;
+			Soa<T, Gp::NR>::load(Smu, g.V, s, a.v);
+			Soa<T, Gp::NR>::load(Tt, g.V, eo_offset<ND>(g, st, mu, r % g.Ld(mu)), b.v);
+			Soa<T, Gp::NR>::load(Smu, g.V, xt, c.v);
+			sum += Gp::retr_nd(Gp::mul(a, b), Gp::mul(d, c));
+		}
+		acc += double(sum);
+	}
+	grid_sum<kBlock>(acc, out);
+}
+
 template <int GRP, class T, int ND>
 __global__ void __launch_bounds__(kBlock) k_staple_sum(Geom g, int mu, T const *__restrict__ U, T *__restrict__ S)
 {
@@ -1715,6 +1780,27 @@ template <int GRP, class T, int ND> struct Ops
 		MESH_LAUNCH_CHECK();
 	}
 
+	// Wilson loops: one line extension / the r x t loop sum (4D only)
+	static void line_extend(Field const &U, int dir, int n, void const *Lprev, void *Lout)
+	{
+		if constexpr (ND == 4)
+		{
+			auto &c = *U.ctx;
+			k_line_extend<GRP, T, ND><<<blocks(c, U.geom.V), kBlock, 0, c.stream>>>(
+			    U.geom, dir, n, static_cast<T const *>(Lprev), static_cast<T const *>(U.d), static_cast<T *>(Lout));
+			MESH_LAUNCH_CHECK();
+		}
+	}
+	static void wilson_rt(Field const &U, int r, int t, void const *S, void const *Tt, RedSlot out)
+	{
+		if constexpr (ND == 4)
+		{
+			auto &c = *U.ctx;
+			k_wilson_rt<GRP, T, ND><<<red_blocks(c, U.geom.V), kBlock, 0, c.stream>>>(
+			    U.geom, r, t, static_cast<T const *>(S), static_cast<T const *>(Tt), out);
+			MESH_LAUNCH_CHECK();
+		}
+	}
 	static OpsTable const *table()
 	{
 		static const OpsTable t = {import_,      export_,       set_unit,       random,  random_momenta_dev,       norm2,
@@ -1723,7 +1809,7 @@ template <int GRP, class T, int ND> struct Ops
 		                           landau_theta, landau_deriv,  landau_or_half, reunit_exact,   alg_dot,
 		                           exp_apply,    axpy_alg,      gauge_transform, tune,
 		                           hmc_plaquette, hmc_evolve,   hmc_momentum_step, hmc_tune,
-		                           hmc_md_step,   hmc_tune_md};
+		                           hmc_md_step,   hmc_tune_md,  line_extend,    wilson_rt};
 		return &t;
 	}
 };

@@ -601,6 +601,19 @@ int oracle_mlp_grad(int n, float const *x, float const *target, float const *par
 	return guarded([&] { *loss = mlp_loss_grad(n, x, target, params, width, grad); });
 }
 
+int oracle_wilson_loops(int grp, int prec, int nd, int const *dims, void const *U, int R, int T, double *out)
+{
+	return guarded([&] {
+		Grid g(nd, dims);
+		if (nd != 4 || R < 1 || T < 1)
+			throw std::runtime_error("Wilson loops need a 4D grid and R, T >= 1");
+		dispatch(grp, prec, [&](auto tag) {
+			using G = decltype(tag);
+			wilson_loops(g, load_stack<G>(g, nd, U), R, T, out);
+		});
+	});
+}
+
 } // extern "C"
 
 // ---- timing of the restated reference path (CPU baseline) ------------------

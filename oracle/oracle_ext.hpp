@@ -15,7 +15,12 @@
 //     (1988) 1581) with a per-momentum multiplier table;
 //   * a direct multi-dimensional DFT;
 //   * the 3-layer tanh MLP of the learned spectral multiplier, with its
-//     mean-squared-error loss and gradient in double precision.
+//     mean-squared-error loss and gradient in double precision;
+//   * rectangular Wilson loops r x t in the planes (mu, 3), mu < 3, as in the
+//     legacy src/old/mesh/wilson.cpp:40-75 (spatial line of r links, temporal
+//     line of t links; sum over sites and the three spatial directions),
+//     normalised like the plaquette (ReTr / Nc), every loop walked link by
+//     link.
 #pragma once
 
 #include "oracle.hpp"
@@ -23,6 +28,45 @@
 #include <complex>
 
 namespace oracle {
+
+// ---- Wilson loops ------------------------------------------------------------
+
+// W(r, t) = sum_x sum_{mu<3} ReTr(S_mu^r(x) T^t(x + r mu) S_mu^r(x + t 3)^+ T^t(x)^+) / (3 V Nc)
+// for r = 1..R, t = 1..T (out[(r-1) T + (t-1)]); S^r: product of r links in
+// direction mu, T^t: product of t links in direction 3. Each loop is walked
+// link by link (no shared line products), in double precision.
+template <class G>
+inline void wilson_loops(Grid const &g, GaugeField<G> const &U, int R, int T, double *out)
+{
+	using real = typename traits<G>::real;
+	std::vector<double> acc(size_t(R) * T, 0.0);
+	for (size_t x = 0; x < g.V; ++x)
+		for (int mu = 0; mu < 3; ++mu)
+			for (int r = 1; r <= R; ++r)
+				for (int t = 1; t <= T; ++t)
+				{
+					G w = unit<G>();
+					size_t y = x;
+					for (int k = 0; k < r; ++k, y = g.shift(y, mu, 1))
+						w = w * U[mu][y];
+					for (int k = 0; k < t; ++k, y = g.shift(y, 3, 1))
+						w = w * U[3][y];
+					for (int k = 0; k < r; ++k)
+					{
+						y = g.shift(y, mu, -1);
+						w = w * adj(U[mu][y]);
+					}
+					for (int k = 0; k < t; ++k)
+					{
+						y = g.shift(y, 3, -1);
+						w = w * adj(U[3][y]);
+					}
+					acc[size_t(r - 1) * T + (t - 1)] += double(real(real_trace(w)));
+				}
+	double norm = 3.0 * double(g.V) * double(traits<G>::Nc);
+	for (size_t k = 0; k < acc.size(); ++k)
+		out[k] = acc[k] / norm;
+}
 
 // ---- gauge-fixed links and the Landau-gauge divergence --------------------
 

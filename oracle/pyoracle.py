@@ -51,6 +51,7 @@ def lib():
             "oracle_make_deltas": (I, [C.c_char_p, D, I, DP, I]),
             "oracle_plaquette": (I, [I, I, I, IP, P, DP]),
             "oracle_wilson_action": (I, [I, I, I, IP, P, D, DP]),
+            "oracle_wilson_loops": (I, [I, I, I, IP, P, I, I, P]),
             "oracle_staple_sum": (I, [I, I, I, IP, P, I, P]),
             "oracle_wilson_deriv": (I, [I, I, I, IP, P, I, D, P]),
             "oracle_evolve": (I, [I, I, I, IP, P, P, D]),
@@ -177,6 +178,15 @@ def plaquette(group, prec, dims, U):
     out = C.c_double()
     _chk(lib().oracle_plaquette(group, prec, nd, d, _ptr(np.ascontiguousarray(U)), C.byref(out)))
     return out.value
+
+
+def wilson_loops(group, prec, dims, U, R, T):
+    """W(r, t), r = 1..R, t = 1..T: rectangular loops in the planes (mu, 3),
+    ReTr / Nc averaged over sites and mu < 3 (array [R, T])"""
+    nd, d = _dims(dims)
+    out = np.zeros((R, T), dtype=np.float64)
+    _chk(lib().oracle_wilson_loops(group, prec, nd, d, _ptr(np.ascontiguousarray(U)), R, T, _ptr(out)))
+    return out
 
 
 def wilson_action(group, prec, dims, U, beta):

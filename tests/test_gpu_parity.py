@@ -447,3 +447,27 @@ def test_errors_are_status_codes(ctx):
     assert e.value.code == 1
     with pytest.raises(mg.MeshError):
         mg.run_hmd(a, mg.Momenta(ctx, 3, 2, mg.Grid([4, 4, 4, 4])), 6.0, [0.1, 0.1])
+
+
+# ---------------------------------------------------------------------------
+# Wilson loops (legacy src/old/mesh/wilson.cpp:40-75)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("g,p", CASES)
+def test_wilson_loops_vs_oracle(ctx, oracle, g, p):
+    """W(r, t) for r = 1..4, t = 1..6 on an asymmetric lattice (lines that
+    wrap around the spatial extents included) against the oracle, which walks
+    every loop link by link"""
+    dims = [4, 6, 4, 6]
+    U64 = thermal(oracle, g, dims)
+    U = gauge(ctx, g, p, dims, U64.astype(mg.real_dtype(p)))
+    W = mg.wilson_loops(U, 4, 6)
+    Wo = oracle.wilson_loops(g, 2, dims, U64, 4, 6)
+    assert np.max(np.abs(W - Wo)) < (1e-13 if p == 2 else 2e-6)
+    assert mg.wilson_loops(U, 1, 1)[0, 0] == pytest.approx(W[0, 0], abs=1e-15 if p == 2 else 1e-7)
+
+
+def test_wilson_loops_argument_errors(ctx):
+    U = mg.GaugeField(ctx, 3, 1, mg.Grid([4, 4, 4, 4]))
+    for r, t in ((0, 1), (5, 1), (1, 0), (1, 5)):
+        with pytest.raises(mg.MeshError):
+            mg.wilson_loops(U, r, t)

@@ -131,6 +131,25 @@ def test_gauge_invariance(oracle):
         assert oracle.plaquette(g, 2, dims, Ug) == pytest.approx(oracle.plaquette(g, 2, dims, U), abs=1e-13)
 
 
+def test_wilson_loops_oracle_identities(oracle):
+    """Wilson loops of the oracle: 1 on a cold start, gauge invariant, and
+    W(1, 1) the mean plaquette of the planes (mu, 3): with the spatial links
+    set to 1 the three spatial planes contribute 1 each to the plaquette, so
+    W(1, 1) = 2 plaquette - 1"""
+    dims = [4, 4, 4, 6]
+    for g in (1, 2, 3):
+        assert np.all(oracle.wilson_loops(g, 2, dims, oracle.unit_gauge(g, 2, dims), 3, 6) == 1.0)
+        U = oracle.random_gauge(g, 2, dims, 3)
+        W = oracle.wilson_loops(g, 2, dims, U, 3, 6)
+        Ug = oracle.gauge_transform(g, 2, dims, U, oracle.random_transform(g, 2, dims, 5))
+        assert np.max(np.abs(oracle.wilson_loops(g, 2, dims, Ug, 3, 6) - W)) < 1e-13
+        Us = U.copy()
+        Us[:3] = oracle.unit_gauge(g, 2, dims)[:3]
+        p = oracle.plaquette(g, 2, dims, Us)  # 3 trivial planes (= 1) and 3 planes (mu, 3)
+        w11 = oracle.wilson_loops(g, 2, dims, Us, 1, 1)[0, 0]
+        assert w11 == pytest.approx(2 * p - 1, abs=1e-13)
+
+
 def test_landau_overrelaxation_converges(oracle):
     dims = [4, 4, 4, 4]
     for g in (1, 2, 3):
