@@ -48,11 +48,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattice", type=int, default=32,
                     help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
-    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson"], default="hmc",
+    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson", "heatbath"], default="hmc",
                     help="hmc: the headline line; batch: 64 SU(2) replicas in one persistent launch against 64 "
                          "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
                          "(plain and learned multiplier); wilson: all r x t Wilson loops of a thermalised "
-                         "configuration")
+                         "configuration; heatbath: heat-bath + overrelaxation sweeps")
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
     ap.add_argument("--fp64", action="store_true",
                     help="hmc workload: the plain all-FP64 chain (links, momenta, force in FP64) instead of the "
@@ -463,6 +463,52 @@ def run_batch(args):
     return 0
 
 
+def run_heatbath(args):
+    """Heat-bath + overrelaxation updates of SU(3) L^4 at beta = 6.0 in FP32
+    (one heat-bath and three overrelaxation sweeps per step, from a cold start
+    after `therm` such steps): link updates per second, and the bytes every
+    link update must move (the link read and written, 2 x 72 B; the staple's
+    neighbour links come from the caches) per second."""
+    import torch
+
+    import mesh_gb300 as mg
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    ctx = mg.Context(0, stream.cuda_stream)
+    L = args.lattice
+    U = mg.GaugeField(ctx, 3, mg.F32, mg.Grid([L] * 4)).set_unit()
+    n_or = 3
+
+    def step(k):
+        mg.heatbath_sweep(U, 6.0, 7, k)
+        for _ in range(n_or):
+            mg.overrelax_sweep(U)
+
+    therm = min(args.therm, 50)
+    for k in range(therm + args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        step(therm + args.warmup + k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dt = e0.elapsed_time(e1) / 1000.0 / args.steps
+    links = 4 * L ** 4
+    upd = links * (1 + n_or) / dt
+    peak, _ = measured_peaks()
+    out = {"metric": "SU(3) heat-bath + overrelaxation link updates/s", "value": upd, "unit": "link-updates/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+           "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"su3_heatbath_{L}^4_beta6.0_1hb_{n_or}or", "start": f"cold, {therm} steps"},
+           "effective_GBps": upd * 144 / 1e9, "peak_GBps": peak, "plaquette": mg.plaquette(U),
+           "gpu_launches": 8 * (1 + n_or) * args.steps}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_wilson(args):
     """All rectangular Wilson loops W(r, t), r = 1..L/2, t = 1..L, of a
     thermalised SU(3) L^4 beta = 6.0 configuration (mixed-precision HMC,
@@ -547,6 +593,8 @@ def main():
         return run_landau(args)
     if args.workload == "wilson":
         return run_wilson(args)
+    if args.workload == "heatbath":
+        return run_heatbath(args)
     return run_ours(args)
 
 

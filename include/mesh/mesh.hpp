@@ -281,6 +281,14 @@ template <class G> double wilsonAction(GaugeField<G> const &U, double beta)
 	check(mesh_wilson_action(U.get(), beta, &s));
 	return s;
 }
+// WilsonAction<G>::sweep / GaugeAction<G>::thermalize and overrelax
+// (src/old/wilson.cpp:15-60, src/old/mesh/gauge_action.h:42-73): one
+// heat-bath or overrelaxation sweep over every link
+template <class G> void thermalize(GaugeField<G> &U, double beta, uint64_t seed, uint64_t sweep)
+{
+	check(mesh_heatbath_sweep(U.get(), beta, seed, sweep));
+}
+template <class G> void overrelax(GaugeField<G> &U) { check(mesh_overrelax_sweep(U.get())); }
 // wilson(const Mesh<G>&, int maxN) of src/old/mesh/wilson.cpp:40-75: the
 // rectangular loops (n, t, W) for n = 1..maxN, t = 1..maxT (default: L3)
 template <class G>

@@ -153,6 +153,22 @@ int mesh_field_norm2(mesh_field a, double *out);
 int mesh_plaquette(mesh_field U, double *out);
 /* Wilson action (1 - plaquette) * beta * Nd(Nd-1)/2 * V (utils.h:141-146) */
 int mesh_wilson_action(mesh_field U, double beta, double *out);
+/* One heat-bath sweep of the Wilson action at beta over every link: the
+ * legacy WilsonAction<G>::sweep (src/old/wilson.cpp:15-60) and
+ * GaugeAction<G>::thermalize (src/old/mesh/gauge_action.h:42-56). U(1) and
+ * SU(2) links are drawn from their conditional distribution given the staple
+ * sum; SU(3) links by three SU(2) subgroup heat-baths (Cabibbo-Marinari).
+ * Links are updated in checkerboard order (per direction, even then odd
+ * sites); the random numbers are Philox draws addressed by (seed, site,
+ * direction, subgroup, attempt) with counter = sweep, so a sweep number
+ * replays the same update. */
+int mesh_heatbath_sweep(mesh_field U, double beta, uint64_t seed, uint64_t sweep);
+/* One overrelaxation sweep: every link reflected so that ReTr(U S) with its
+ * staple sum S is unchanged (GaugeAction<G>::overrelax,
+ * src/old/mesh/gauge_action.h:59-73; SU(3) through its three SU(2) subgroups,
+ * where the legacy formula would not keep the action). The action is
+ * unchanged up to rounding. */
+int mesh_overrelax_sweep(mesh_field U);
 /* Rectangular Wilson loops W(r, t) for r = 1..max_r, t = 1..max_t in the planes
  * (mu, 3), mu = 0, 1, 2: the legacy wilson() of src/old/mesh/wilson.cpp:40-75
  * (spatial line of r links, temporal line of t links, averaged over sites and

@@ -91,6 +91,8 @@ SIGNATURES = {
     "mesh_plaquette": (_I, [_P, _DP]),
     "mesh_wilson_action": (_I, [_P, _D, _DP]),
     "mesh_wilson_loops": (_I, [_P, _I, _I, _DP]),
+    "mesh_heatbath_sweep": (_I, [_P, _D, C.c_uint64, C.c_uint64]),
+    "mesh_overrelax_sweep": (_I, [_P]),
     "mesh_plaquette_noalloc": (_I, [_I, _I, _I, _I, _I32P, _P, _P, _DP]),
     "mesh_staple_sum": (_I, [_P, _P, _I]),
     "mesh_wilson_deriv": (_I, [_P, _P, _I, _D]),
@@ -410,6 +412,19 @@ def wilson_action(U: Field, beta: float) -> float:
     out = C.c_double()
     _chk(load().mesh_wilson_action(U.h, beta, C.byref(out)))
     return out.value
+
+
+def heatbath_sweep(U: Field, beta: float, seed: int, sweep: int) -> Field:
+    """one heat-bath sweep of the Wilson action (checkerboard order; the
+    random numbers are addressed by seed and sweep number)"""
+    _chk(load().mesh_heatbath_sweep(U.h, beta, seed, sweep))
+    return U
+
+
+def overrelax_sweep(U: Field) -> Field:
+    """one overrelaxation sweep (keeps the action)"""
+    _chk(load().mesh_overrelax_sweep(U.h))
+    return U
 
 
 def wilson_loops(U: Field, max_r: int, max_t: int) -> np.ndarray:

@@ -635,6 +635,27 @@ int mesh_plaquette(mesh_field Uh, double *out)
 	});
 }
 
+int mesh_heatbath_sweep(mesh_field Uh, double beta, uint64_t seed, uint64_t sweep)
+{
+	return api([&] {
+		Field &U = F(Uh);
+		check_gauge(U);
+		require(std::isfinite(beta) && beta >= 0, "beta must be finite and >= 0");
+		DeviceGuard dg(U.ctx->device);
+		ops_for(U).gauge_sweep(U, beta, seed, sweep, false);
+	});
+}
+
+int mesh_overrelax_sweep(mesh_field Uh)
+{
+	return api([&] {
+		Field &U = F(Uh);
+		check_gauge(U);
+		DeviceGuard dg(U.ctx->device);
+		ops_for(U).gauge_sweep(U, 0.0, 0, 0, true);
+	});
+}
+
 int mesh_wilson_loops(mesh_field Uh, int max_r, int max_t, double *out)
 {
 	return api([&] {

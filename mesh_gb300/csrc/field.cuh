@@ -122,6 +122,8 @@ struct OpsTable
 	// Wilson loops (4D): Lout = Lprev U_dir(x + (n-1) dir); sum of the r x t loops
 	void (*line_extend)(Field const &U, int dir, int n, void const *Lprev, void *Lout);
 	void (*wilson_rt)(Field const &U, int r, int t, void const *S, void const *Tt, RedSlot out);
+	// one heat-bath (overrelax = false) or overrelaxation sweep, checkerboard order
+	void (*gauge_sweep)(Field &U, double beta, uint64_t seed, uint64_t ctr, bool overrelax);
 };
 
 // autotuning registry (tune.cu): variant index per kernel/lattice key

@@ -5,6 +5,7 @@
 
 #include "field.cuh"
 #include "group.cuh"
+#include "heatbath.cuh"
 #include "rng.cuh"
 
 #include <string>
@@ -704,6 +705,35 @@ __global__ void __launch_bounds__(NT, MINB)
 	}
 	if (kin.result)
 		grid_sum<NT>(acc, kin);
+}
+
+// ---------------------------------------------------------------------------
+// heat-bath / overrelaxation (legacy src/old/wilson.cpp:15-60,
+// src/old/mesh/gauge_action.h:42-73), checkerboard: the links (x, mu) of one
+// parity do not enter each other's staples (those read U_mu only at x +- nu,
+// of the other parity), so they are updated together
+// ---------------------------------------------------------------------------
+template <int GRP, class T, int ND, bool OR>
+__global__ void __launch_bounds__(kBlock)
+    k_gauge_update(Geom g, int mu, int parity, T *U, double beta, uint64_t seed, uint64_t ctr)
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	LinkLoad<GRP, T, ND> ld{U, g.V};
+	MESH_GRID_LOOP(i, g.Vh)
+	{
+		int64_t s = int64_t(parity) * g.Vh + i;
+		Site<ND> st = site_from_eo<ND>(g, s);
+		E S = staple<GRP, T, ND>(g, st, s, mu, ld);
+		auto v = comp<T, Gp::NR>(U, g.V, mu);
+		E u;
+		v.load(s, u.v);
+		if constexpr (OR)
+			HbUpdate<GRP, T>::overrelax(u, S);
+		else
+			HbUpdate<GRP, T>::heatbath(u, S, beta, HbStream{seed, ctr, uint32_t(st.lex), uint32_t(mu), 0u});
+		v.store(s, u.v);
+	}
 }
 
 // ---------------------------------------------------------------------------
@@ -1780,6 +1810,22 @@ template <int GRP, class T, int ND> struct Ops
 		MESH_LAUNCH_CHECK();
 	}
 
+	// one heat-bath (or overrelaxation) sweep: every direction, both parities
+	static void gauge_sweep(Field &U, double beta, uint64_t seed, uint64_t ctr, bool overrelax)
+	{
+		auto &c = *U.ctx;
+		for (int mu = 0; mu < ND; ++mu)
+			for (int par = 0; par < 2; ++par)
+			{
+				if (overrelax)
+					k_gauge_update<GRP, T, ND, true><<<blocks(c, U.geom.Vh), kBlock, 0, c.stream>>>(
+					    U.geom, mu, par, static_cast<T *>(U.d), beta, seed, ctr);
+				else
+					k_gauge_update<GRP, T, ND, false><<<blocks(c, U.geom.Vh), kBlock, 0, c.stream>>>(
+					    U.geom, mu, par, static_cast<T *>(U.d), beta, seed, ctr);
+				MESH_LAUNCH_CHECK();
+			}
+	}
 	// Wilson loops: one line extension / the r x t loop sum (4D only)
 	static void line_extend(Field const &U, int dir, int n, void const *Lprev, void *Lout)
 	{
@@ -1809,7 +1855,8 @@ template <int GRP, class T, int ND> struct Ops
 		                           landau_theta, landau_deriv,  landau_or_half, reunit_exact,   alg_dot,
 		                           exp_apply,    axpy_alg,      gauge_transform, tune,
 		                           hmc_plaquette, hmc_evolve,   hmc_momentum_step, hmc_tune,
-		                           hmc_md_step,   hmc_tune_md,  line_extend,    wilson_rt};
+		                           hmc_md_step,   hmc_tune_md,  line_extend,    wilson_rt,
+		                           gauge_sweep};
 		return &t;
 	}
 };

@@ -601,6 +601,20 @@ int oracle_mlp_grad(int n, float const *x, float const *target, float const *par
 	return guarded([&] { *loss = mlp_loss_grad(n, x, target, params, width, grad); });
 }
 
+int oracle_gauge_sweep(int grp, int prec, int nd, int const *dims, void *U, double beta, uint64_t seed,
+                       uint64_t ctr, int overrelax)
+{
+	return guarded([&] {
+		Grid g(nd, dims);
+		dispatch(grp, prec, [&](auto tag) {
+			using G = decltype(tag);
+			auto F = load_stack<G>(g, nd, U);
+			gauge_sweep(g, F, beta, seed, ctr, overrelax != 0);
+			store_stack(g, F, U);
+		});
+	});
+}
+
 int oracle_wilson_loops(int grp, int prec, int nd, int const *dims, void const *U, int R, int T, double *out)
 {
 	return guarded([&] {

@@ -16,6 +16,13 @@
 //   * a direct multi-dimensional DFT;
 //   * the 3-layer tanh MLP of the learned spectral multiplier, with its
 //     mean-squared-error loss and gradient in double precision;
+//   * heat-bath and overrelaxation sweeps of the Wilson action, checkerboard
+//     order (direction, then parity), with the per-link updates of the legacy
+//     src/old/wilson.cpp:15-60 and src/old/mesh/gauge_action.h:42-73: SU(2)
+//     Kennedy & Pendleton (Phys. Lett. B 156 (1985) 393) / Creutz (Phys. Rev.
+//     D 21 (1980) 2308), U(1) von Mises by Best & Fisher (Appl. Statist. 28
+//     (1979) 152), SU(3) by Cabibbo-Marinari subgroups; the same Philox streams
+//     as the device;
 //   * rectangular Wilson loops r x t in the planes (mu, 3), mu < 3, as in the
 //     legacy src/old/mesh/wilson.cpp:40-75 (spatial line of r links, temporal
 //     line of t links; sum over sites and the three spatial directions),
@@ -28,6 +35,208 @@
 #include <complex>
 
 namespace oracle {
+
+// ---- heat-bath and overrelaxation -------------------------------------------
+
+constexpr uint32_t TAG_HEATBATH = 5;
+constexpr int HB_TRIES = 24;
+
+struct hb_stream
+{
+	uint64_t seed, ctr;
+	uint32_t site, mu, sub;
+	void draw(uint32_t call, double *u) const
+	{
+		auto r = philox4x32_10(site, (TAG_HEATBATH << 24) | (mu << 8) | (sub << 6) | call, uint32_t(ctr),
+		                       uint32_t(ctr >> 32), uint32_t(seed), uint32_t(seed >> 32));
+		u[0] = u53(r.v[0], r.v[1]);
+		u[1] = u53(r.v[2], r.v[3]);
+	}
+};
+
+// X = (x0, x1, x2, x3) in SU(2) with density exp(alpha x0) (Haar measure)
+inline bool hb_su2(double alpha, hb_stream const &rs, double *x)
+{
+	double x0 = 0;
+	bool ok = false;
+	for (int a = 0; a < HB_TRIES && !ok; ++a)
+	{
+		double u[4];
+		rs.draw(uint32_t(1 + 2 * a), u);
+		rs.draw(uint32_t(2 + 2 * a), u + 2);
+		if (alpha < 1.0)
+		{
+			// Creutz: x from the density exp(alpha x) by inversion, accepted
+			// with probability sqrt(1 - x^2)
+			double t = alpha < 1e-8 ? 2.0 * u[0] - 1.0
+			                        : 1.0 + std::log(u[0] + (1.0 - u[0]) * std::exp(-2.0 * alpha)) / alpha;
+			if (u[1] * u[1] <= 1.0 - t * t)
+				x0 = t, ok = true;
+		}
+		else
+		{
+			// Kennedy-Pendleton in delta = 1 - x0
+			double c = std::cos(M_PI * 2.0 * u[1]);
+			double d = -(std::log(u[0]) + c * c * std::log(u[2])) / alpha;
+			if (u[3] * u[3] <= 1.0 - 0.5 * d)
+				x0 = 1.0 - d, ok = true;
+		}
+	}
+	if (!ok)
+		return false;
+	double u[2];
+	rs.draw(0, u);
+	double ct = 2.0 * u[0] - 1.0, st = std::sqrt(std::max(0.0, 1.0 - ct * ct));
+	double sp = std::sin(M_PI * 2.0 * u[1]), cp = std::cos(M_PI * 2.0 * u[1]);
+	double r = std::sqrt(std::max(0.0, 1.0 - x0 * x0));
+	x[0] = x0;
+	x[1] = r * st * cp;
+	x[2] = r * st * sp;
+	x[3] = r * ct;
+	return true;
+}
+
+// von Mises angle, density exp(kappa cos theta) (Best & Fisher)
+inline bool hb_u1(double kappa, hb_stream const &rs, double *theta)
+{
+	if (kappa < 1e-8)
+	{
+		double u[2];
+		rs.draw(1, u);
+		*theta = M_PI * (2.0 * u[0] - 1.0);
+		return true;
+	}
+	double tau = 1.0 + std::sqrt(1.0 + 4.0 * kappa * kappa);
+	double rho = (tau - std::sqrt(2.0 * tau)) / (2.0 * kappa);
+	double r = (1.0 + rho * rho) / (2.0 * rho);
+	for (int a = 0; a < HB_TRIES; ++a)
+	{
+		double u[4];
+		rs.draw(uint32_t(1 + 2 * a), u);
+		rs.draw(uint32_t(2 + 2 * a), u + 2);
+		double z = std::cos(M_PI * u[0]);
+		double f = (1.0 + r * z) / (r + z);
+		double c = kappa * (r - f);
+		if (c * (2.0 - c) - u[1] > 0.0 || std::log(c / u[1]) + 1.0 - c >= 0.0)
+		{
+			f = std::min(1.0, std::max(-1.0, f));
+			*theta = (u[2] > 0.5 ? 1.0 : -1.0) * std::acos(f);
+			return true;
+		}
+	}
+	return false;
+}
+
+// one link: heat-bath (or, with OR, the action-keeping reflection) from the
+// staple sum S
+template <class T> inline void hb_link(cplx<T> &u, cplx<T> const &S, double beta, hb_stream rs, bool OR)
+{
+	double sr = S.re, si = S.im, k = std::sqrt(sr * sr + si * si);
+	if (OR)
+	{
+		if (!(k > 0))
+			return;
+		// U' = conj(v)^2 conj(U)
+		std::complex<double> v(sr / k, si / k), uu(u.re, u.im);
+		std::complex<double> r = std::conj(v) * std::conj(v) * std::conj(uu);
+		u = {T(r.real()), T(r.imag())};
+		return;
+	}
+	double th;
+	if (!hb_u1(beta * k, rs, &th))
+		return;
+	std::complex<double> v = k > 0 ? std::complex<double>(sr / k, si / k) : std::complex<double>(1, 0);
+	std::complex<double> r = std::complex<double>(std::cos(th), std::sin(th)) * std::conj(v);
+	u = {T(r.real()), T(r.imag())};
+}
+template <class T> inline void hb_link(quat<T> &u, quat<T> const &S, double beta, hb_stream rs, bool OR)
+{
+	double k = std::sqrt(double(S.re) * S.re + double(S.im1) * S.im1 + double(S.im2) * S.im2 + double(S.im3) * S.im3);
+	if (OR)
+	{
+		if (!(k > 0))
+			return;
+		quat<T> vd = conj(quat<T>{T(S.re / k), T(S.im1 / k), T(S.im2 / k), T(S.im3 / k)});
+		u = project_on_group_fast(vd * conj(u) * vd);
+		return;
+	}
+	double x[4];
+	if (!hb_su2(beta * k, rs, x))
+		return;
+	quat<T> X{T(x[0]), T(x[1]), T(x[2]), T(x[3])};
+	quat<T> v = k > 0 ? quat<T>{T(S.re / k), T(S.im1 / k), T(S.im2 / k), T(S.im3 / k)} : unit<quat<T>>();
+	u = project_on_group_fast(X * conj(v));
+}
+template <class T> inline void hb_link(mat3<T> &u, mat3<T> const &S, double beta, hb_stream rs, bool OR)
+{
+	using C = std::complex<double>;
+	auto W = u * S;
+	static const int SI[3] = {0, 1, 0}, SJ[3] = {1, 2, 2};
+	for (int sg = 0; sg < 3; ++sg)
+	{
+		int i = SI[sg], j = SJ[sg];
+		// SU(2)-like part [[A, B], [-B*, A*]] of the block (i, j) of W
+		C A = 0.5 * (C(W.m[i][i].re, W.m[i][i].im) + std::conj(C(W.m[j][j].re, W.m[j][j].im)));
+		C B = 0.5 * (C(W.m[i][j].re, W.m[i][j].im) - std::conj(C(W.m[j][i].re, W.m[j][i].im)));
+		double k = std::sqrt(std::norm(A) + std::norm(B));
+		if (!(k > 0))
+			continue;
+		A /= k;
+		B /= k;
+		C xp, xq; // X = [[xp, xq], [-xq*, xp*]]
+		if (OR)
+		{
+			xp = std::conj(A); // X = v^dagger
+			xq = -B;
+		}
+		else
+		{
+			rs.sub = uint32_t(sg);
+			double x[4];
+			if (!hb_su2(2.0 * beta * k / 3.0, rs, x))
+				continue;
+			xp = C(x[0], x[3]);
+			xq = C(x[2], x[1]);
+		}
+		// R = X v^dagger, v^dagger = [[A*, -B], [B*, A]]
+		C p = xp * std::conj(A) + xq * std::conj(B);
+		C q = -xp * B + xq * A;
+		auto left = [&](mat3<T> &M) {
+			for (int c = 0; c < 3; ++c)
+			{
+				C x(M.m[i][c].re, M.m[i][c].im), y(M.m[j][c].re, M.m[j][c].im);
+				C nx = p * x + q * y, ny = -std::conj(q) * x + std::conj(p) * y;
+				M.m[i][c] = {T(nx.real()), T(nx.imag())};
+				M.m[j][c] = {T(ny.real()), T(ny.imag())};
+			}
+		};
+		left(u);
+		left(W);
+	}
+	u = project_on_group_fast(u);
+}
+
+// one sweep: for mu, for parity (0, 1), every link (x, mu) with parity(x) =
+// parity from the staples of the current links; counter = sweep number
+template <class G>
+inline void gauge_sweep(Grid const &g, GaugeField<G> &U, double beta, uint64_t seed, uint64_t ctr, bool OR)
+{
+	for (int mu = 0; mu < g.nd; ++mu)
+		for (int par = 0; par < 2; ++par)
+		{
+			auto S = stapleSum(g, U, mu);
+			site_loop(g.V, [&](size_t r) {
+				int x[4];
+				g.coords(r, x);
+				int p = 0;
+				for (int i = 0; i < g.nd; ++i)
+					p += x[i];
+				if ((p & 1) != par)
+					return;
+				hb_link(U[mu][r], S[r], beta, hb_stream{seed, ctr, uint32_t(r), uint32_t(mu), 0}, OR);
+			});
+		}
+}
 
 // ---- Wilson loops ------------------------------------------------------------
 

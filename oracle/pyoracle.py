@@ -52,6 +52,7 @@ def lib():
             "oracle_plaquette": (I, [I, I, I, IP, P, DP]),
             "oracle_wilson_action": (I, [I, I, I, IP, P, D, DP]),
             "oracle_wilson_loops": (I, [I, I, I, IP, P, I, I, P]),
+            "oracle_gauge_sweep": (I, [I, I, I, IP, P, D, U64, U64, I]),
             "oracle_staple_sum": (I, [I, I, I, IP, P, I, P]),
             "oracle_wilson_deriv": (I, [I, I, I, IP, P, I, D, P]),
             "oracle_evolve": (I, [I, I, I, IP, P, P, D]),
@@ -178,6 +179,15 @@ def plaquette(group, prec, dims, U):
     out = C.c_double()
     _chk(lib().oracle_plaquette(group, prec, nd, d, _ptr(np.ascontiguousarray(U)), C.byref(out)))
     return out.value
+
+
+def gauge_sweep(group, prec, dims, U, beta, seed, counter, overrelax=False):
+    """one heat-bath (or overrelaxation) sweep in checkerboard order; returns
+    the new links"""
+    nd, d = _dims(dims)
+    U = np.ascontiguousarray(U.copy())
+    _chk(lib().oracle_gauge_sweep(group, prec, nd, d, _ptr(U), beta, seed, counter, 1 if overrelax else 0))
+    return U
 
 
 def wilson_loops(group, prec, dims, U, R, T):

@@ -107,13 +107,16 @@ def test_cpp_dropin_app_compiles(libpath, tmp_path):
 
 
 def test_cpp_wilson_loops_instantiate(libpath, tmp_path):
-    """the drop-in wilson() (legacy src/old/mesh/wilson.cpp:40-75) compiles
-    for every group and precision"""
+    """the drop-in wilson(), thermalize() and overrelax() (legacy
+    src/old/mesh/wilson.cpp:40-75, src/old/wilson.cpp, gauge_action.h)
+    compile"""
     src = tmp_path / "w.cpp"
     src.write_text('#include "mesh/mesh.hpp"\n'
                    "template std::vector<std::tuple<int, int, double>> mesh::wilson(mesh::GaugeField<mesh::U1<float>> const &, int, int);\n"
                    "template std::vector<std::tuple<int, int, double>> mesh::wilson(mesh::GaugeField<mesh::SU2<double>> const &, int, int);\n"
-                   "template std::vector<std::tuple<int, int, double>> mesh::wilson(mesh::GaugeField<mesh::SU3<float>> const &, int, int);\n")
+                   "template std::vector<std::tuple<int, int, double>> mesh::wilson(mesh::GaugeField<mesh::SU3<float>> const &, int, int);\n"
+                   "template void mesh::thermalize(mesh::GaugeField<mesh::SU3<double>> &, double, uint64_t, uint64_t);\n"
+                   "template void mesh::overrelax(mesh::GaugeField<mesh::U1<float>> &);\n")
     r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Werror", "-c", "-I", os.path.join(ROOT, "include"),
                         str(src), "-o", str(tmp_path / "w.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

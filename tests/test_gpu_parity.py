@@ -471,3 +471,58 @@ def test_wilson_loops_argument_errors(ctx):
     for r, t in ((0, 1), (5, 1), (1, 0), (1, 5)):
         with pytest.raises(mg.MeshError):
             mg.wilson_loops(U, r, t)
+
+
+# ---------------------------------------------------------------------------
+# heat-bath and overrelaxation (legacy src/old/wilson.cpp:15-60,
+# src/old/mesh/gauge_action.h:42-73)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("g", [1, 2, 3])
+def test_heatbath_and_overrelaxation_fp64_vs_oracle(ctx, oracle, g):
+    """FP64 heat-bath sweeps (same Philox streams, same checkerboard order)
+    and an overrelaxation sweep against the oracle; the overrelaxation sweep
+    keeps the action"""
+    dims = [4, 4, 4, 6]
+    U64 = thermal(oracle, g, dims)
+    U = gauge(ctx, g, 2, dims, U64)
+    for k in range(2):
+        mg.heatbath_sweep(U, BETA[g], 21, k)
+        U64 = oracle.gauge_sweep(g, 2, dims, U64, BETA[g], 21, k)
+    assert rel(U.export(), U64) < 1e-12
+    p0 = mg.plaquette(U)
+    mg.overrelax_sweep(U)
+    U64 = oracle.gauge_sweep(g, 2, dims, U64, BETA[g], 0, 0, overrelax=True)
+    assert rel(U.export(), U64) < 1e-12
+    assert abs(mg.plaquette(U) - p0) < 1e-13
+
+
+@pytest.mark.parametrize("g", [1, 2, 3])
+def test_overrelaxation_keeps_action_fp32(ctx, oracle, g):
+    dims = [8, 8, 8, 8]
+    U = gauge(ctx, g, 1, dims, thermal(oracle, g, dims).astype(np.float32))
+    p0 = mg.plaquette(U)
+    mg.overrelax_sweep(U)
+    assert abs(mg.plaquette(U) - p0) < 2e-6
+
+
+def test_heatbath_equilibrium_matches_hmc(ctx):
+    """SU(3) 8^4 beta = 5.7, FP32: the equilibrium plaquette of heat-bath +
+    overrelaxation sweeps and of HMC trajectories agree within their
+    statistical errors (two Markov chains with the same distribution)"""
+    dims = [8, 8, 8, 8]
+    U = mg.GaugeField(ctx, 3, 1, mg.Grid(dims)).set_unit()
+    ph = []
+    for k in range(160):
+        mg.heatbath_sweep(U, 5.7, 3, k)
+        for _ in range(3):
+            mg.overrelax_sweep(U)
+        if k >= 40:
+            ph.append(mg.plaquette(U))
+    h = mg.Hmc(ctx, 3, 1, mg.Grid(dims), seed=4)
+    h.cold_start()
+    h.run(5.7, mg.make_deltas("2mn", 0.5, 10), 160, use_graph=True)
+    pm = h.history()["plaq_history"][40:]
+    ph, pm = np.array(ph), np.array(pm)
+    # errors from blocks of 20 (autocorrelations)
+    err = np.hypot(ph.reshape(6, 20).mean(1).std() / np.sqrt(6), pm.reshape(6, 20).mean(1).std() / np.sqrt(6))
+    assert abs(ph.mean() - pm.mean()) < 4 * err + 1e-3, (ph.mean(), pm.mean(), err)

@@ -150,6 +150,25 @@ def test_wilson_loops_oracle_identities(oracle):
         assert w11 == pytest.approx(2 * p - 1, abs=1e-13)
 
 
+def test_heatbath_strong_coupling_and_overrelaxation(oracle):
+    """The oracle's heat-bath at small beta reproduces the strong-coupling
+    plaquette (U(1): beta/2, SU(2): beta/4, SU(3): beta/18 + beta^2/216, the
+    line sweep_beta plots, src/apps/sweep_beta.cpp:91), and an
+    overrelaxation sweep keeps the action"""
+    dims = [4, 4, 4, 4]
+    for g, beta, pred in ((1, 0.4, 0.2 - 0.4 ** 3 / 16), (2, 0.8, 0.2), (3, 1.2, 1.2 / 18 + 1.44 / 216)):
+        U = oracle.unit_gauge(g, 2, dims)
+        ps = []
+        for k in range(60):
+            U = oracle.gauge_sweep(g, 2, dims, U, beta, 11, k)
+            if k >= 10:
+                ps.append(oracle.plaquette(g, 2, dims, U))
+        assert abs(np.mean(ps) - pred) < 0.012, (g, np.mean(ps), pred)
+        p0 = oracle.plaquette(g, 2, dims, U)
+        U2 = oracle.gauge_sweep(g, 2, dims, U, beta, 0, 0, overrelax=True)
+        assert abs(oracle.plaquette(g, 2, dims, U2) - p0) < 1e-13 and np.max(np.abs(U2 - U)) > 0.1
+
+
 def test_landau_overrelaxation_converges(oracle):
     dims = [4, 4, 4, 4]
     for g in (1, 2, 3):
