@@ -516,13 +516,16 @@ def test_heatbath_equilibrium_matches_hmc(ctx):
         mg.heatbath_sweep(U, 5.7, 3, k)
         for _ in range(3):
             mg.overrelax_sweep(U)
-        if k >= 40:
+        if k >= 60:
             ph.append(mg.plaquette(U))
+    # HMC from a hot start (from a cold start at this beta the first
+    # trajectories have dH ~ +9 and are all rejected)
     h = mg.Hmc(ctx, 3, 1, mg.Grid(dims), seed=4)
-    h.cold_start()
+    h.randomize_gauge_field()
     h.run(5.7, mg.make_deltas("2mn", 0.5, 10), 160, use_graph=True)
-    pm = h.history()["plaq_history"][40:]
+    pm = h.history()["plaq_history"][60:]
+    assert h.history()["accept_history"][60:].mean() > 0.5
     ph, pm = np.array(ph), np.array(pm)
     # errors from blocks of 20 (autocorrelations)
-    err = np.hypot(ph.reshape(6, 20).mean(1).std() / np.sqrt(6), pm.reshape(6, 20).mean(1).std() / np.sqrt(6))
+    err = np.hypot(ph.reshape(5, 20).mean(1).std() / np.sqrt(5), pm.reshape(5, 20).mean(1).std() / np.sqrt(5))
     assert abs(ph.mean() - pm.mean()) < 4 * err + 1e-3, (ph.mean(), pm.mean(), err)
