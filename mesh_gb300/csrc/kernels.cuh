@@ -731,7 +731,7 @@ __global__ void __launch_bounds__(kBlock)
 		if constexpr (OR)
 			HbUpdate<GRP, T>::overrelax(u, S);
 		else
-			HbUpdate<GRP, T>::heatbath(u, S, beta, HbStream{seed, ctr, uint32_t(st.lex), uint32_t(mu), 0u});
+			HbUpdate<GRP, T>::heatbath(u, S, T(beta), HbStream{seed, ctr, uint32_t(st.lex), uint32_t(mu), 0u});
 		v.store(s, u.v);
 	}
 }

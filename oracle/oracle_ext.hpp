@@ -96,14 +96,16 @@ inline bool hb_su2(double alpha, hb_stream const &rs, double *x)
 	return true;
 }
 
-// von Mises angle, density exp(kappa cos theta) (Best & Fisher)
-inline bool hb_u1(double kappa, hb_stream const &rs, double *theta)
+// von Mises angle, density exp(kappa cos theta) (Best & Fisher), returned
+// as its cosine and sine
+inline bool hb_u1(double kappa, hb_stream const &rs, double *cs, double *sn)
 {
 	if (kappa < 1e-8)
 	{
 		double u[2];
 		rs.draw(1, u);
-		*theta = M_PI * (2.0 * u[0] - 1.0);
+		*sn = std::sin(M_PI * (2.0 * u[0] - 1.0));
+		*cs = std::cos(M_PI * (2.0 * u[0] - 1.0));
 		return true;
 	}
 	double tau = 1.0 + std::sqrt(1.0 + 4.0 * kappa * kappa);
@@ -120,7 +122,8 @@ inline bool hb_u1(double kappa, hb_stream const &rs, double *theta)
 		if (c * (2.0 - c) - u[1] > 0.0 || std::log(c / u[1]) + 1.0 - c >= 0.0)
 		{
 			f = std::min(1.0, std::max(-1.0, f));
-			*theta = (u[2] > 0.5 ? 1.0 : -1.0) * std::acos(f);
+			*cs = f;
+			*sn = (u[2] > 0.5 ? 1.0 : -1.0) * std::sqrt(std::max(0.0, 1.0 - f * f));
 			return true;
 		}
 	}
@@ -142,11 +145,11 @@ template <class T> inline void hb_link(cplx<T> &u, cplx<T> const &S, double beta
 		u = {T(r.real()), T(r.imag())};
 		return;
 	}
-	double th;
-	if (!hb_u1(beta * k, rs, &th))
+	double cs, sn;
+	if (!hb_u1(beta * k, rs, &cs, &sn))
 		return;
 	std::complex<double> v = k > 0 ? std::complex<double>(sr / k, si / k) : std::complex<double>(1, 0);
-	std::complex<double> r = std::complex<double>(std::cos(th), std::sin(th)) * std::conj(v);
+	std::complex<double> r = std::complex<double>(cs, sn) * std::conj(v);
 	u = {T(r.real()), T(r.imag())};
 }
 template <class T> inline void hb_link(quat<T> &u, quat<T> const &S, double beta, hb_stream rs, bool OR)
