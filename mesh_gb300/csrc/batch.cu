@@ -19,6 +19,12 @@
 // block adds, for each replica, the partials of exactly the blocks that
 // covered it (deterministic for a given batch).
 //
+// MD steps: each momentum step runs fused with the link update after it in
+// one launch over the sites of every replica (the single-lattice
+// thread-per-site body, site_md), reading the proposal from Unew or Ut and
+// writing it to the other; a one-thread-per-replica kernel swaps the two
+// pointers when the proposal ends in Ut.
+//
 // Accept: the Metropolis kernel (one thread per replica) swaps the
 // replica's U and U_new pointers in the descriptor table instead of copying
 // the proposal, so an accepted trajectory costs no link traffic.
@@ -47,6 +53,7 @@ struct BatchRep
 	Geom g;
 	void *U;       // accepted links
 	void *Unew;    // proposal (swapped with U on accept)
+	void *Ut;      // second proposal buffer of the fused MD steps (swapped with Unew)
 	void *P;       // momenta
 	uint64_t seed; // Philox key of the replica's momentum and Metropolis streams
 	int64_t lchunk0, schunk0; // first chunk of the replica's links / sites
@@ -271,6 +278,37 @@ __global__ void __launch_bounds__(kChunk)
 	});
 }
 
+// P -= (beta_r / (2 Nc)) dp proj(U S) fused with U' = exp(du P) U for the four
+// links of every site; reads the proposal from Unew (flip = 0) or Ut (flip =
+// 1) and writes it to the other; with KIN also the kinetic sums
+template <int GRP, class T, bool KIN>
+__global__ void __launch_bounds__(kChunk)
+    kb_md(BatchSpace sp, double const *__restrict__ beta, double dp, double du, int flip, int reunit, BatchRed kin)
+{
+	using Gp = Group<GRP, T>;
+	constexpr int F2 = (GRP == SU3 && sizeof(T) == 4) ? 1 : 0;
+	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s) {
+		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(flip ? rep.Ut : rep.Unew), rep.g.V};
+		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
+		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true>(rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
+		                                                          static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
+		                                                          reunit);
+		return KIN ? k : 0.0;
+	});
+}
+
+// the proposal back in Unew after an odd number of fused steps
+__global__ void kb_swap_proposal(BatchRep *reps, int R)
+{
+	int r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= R)
+		return;
+	void *t = reps[r].Unew;
+	reps[r].Unew = reps[r].Ut;
+	reps[r].Ut = t;
+}
+
 // per-replica plaquette trace sums of U (NEW: of U_new)
 template <int GRP, class T, bool NEW> __global__ void __launch_bounds__(kChunk) kb_plaquette(BatchSpace sp, BatchRed out)
 {
@@ -333,7 +371,9 @@ struct BatchOps
 	void (*evolve)(cudaStream_t, unsigned, BatchSpace, double, bool first, bool reunit);
 	void (*force)(cudaStream_t, unsigned, BatchSpace, double const *, double, BatchRed, bool kin);
 	void (*plaquette)(cudaStream_t, unsigned, BatchSpace, BatchRed, bool on_new);
-	int (*occupancy)(int which); // resident blocks per SM of kernel `which` (0 links-type, 1 force, 2 sites)
+	void (*md)(cudaStream_t, unsigned, BatchSpace, double const *, double dp, double du, bool flip, bool reunit,
+	           BatchRed, bool kin);
+	int (*occupancy)(int which); // resident blocks per SM of kernel `which` (0 links-type, 1 force, 2 sites, 3 md)
 };
 
 template <int GRP, class T> struct BatchImpl
@@ -382,11 +422,22 @@ template <int GRP, class T> struct BatchImpl
 			kb_plaquette<GRP, T, false><<<g, kChunk, 0, st>>>(sp, out);
 		MESH_LAUNCH_CHECK();
 	}
+	static void md(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double dp, double du, bool flip,
+	               bool reunit, BatchRed kin, bool with_kin)
+	{
+		if (with_kin)
+			kb_md<GRP, T, true><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+		else
+			kb_md<GRP, T, false><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+		MESH_LAUNCH_CHECK();
+	}
 	static int occupancy(int which)
 	{
 		int n = 0;
 		cudaError_t e;
-		if (which == 1)
+		if (which == 3)
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true>, kChunk, 0);
+		else if (which == 1)
 			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_force<GRP, T, true>, kChunk, 0);
 		else if (which == 2)
 			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_plaquette<GRP, T, true>, kChunk, 0);
@@ -395,7 +446,7 @@ template <int GRP, class T> struct BatchImpl
 		MESH_CUDA(e);
 		return n;
 	}
-	static constexpr BatchOps ops{random_links, unit_links, refresh, evolve, force, plaquette, occupancy};
+	static constexpr BatchOps ops{random_links, unit_links, refresh, evolve, force, plaquette, md, occupancy};
 };
 
 BatchOps const &batch_ops(int group, int prec)
@@ -417,7 +468,7 @@ struct mesh_batch_s
 	int group = 0, prec = 0, R = 0;
 	std::vector<int32_t> dims;  // R x 4
 	std::vector<BatchRep> reps; // host copy at creation (initial pointers)
-	void *bufU = nullptr, *bufUnew = nullptr, *bufP = nullptr;
+	void *bufU = nullptr, *bufUnew = nullptr, *bufUt = nullptr, *bufP = nullptr;
 	BatchRep *d_reps = nullptr;
 	HmcDev *d_dev = nullptr;
 	HmcRecordDev *d_hist = nullptr;
@@ -426,7 +477,8 @@ struct mesh_batch_s
 	double *d_part = nullptr, *d_res = nullptr; // partials [G][R]; results [4][R]
 	unsigned *d_cnt = nullptr;
 	BatchSpace links{}, sites{};
-	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
+	unsigned g_links = 0, g_force = 0, g_sites = 0, g_md = 0; // grids (links space uses g_links/g_force chunks)
+	BatchSpace md_sp{};
 	BatchSpace force_sp{};
 	int64_t count = 0;
 	bool S_valid = false;
@@ -458,7 +510,7 @@ struct mesh_batch_s
 		cudaSetDevice(ctx->device);
 		cudaStreamSynchronize(ctx->stream);
 		drop_graph();
-		for (void *p : {bufU, bufUnew, bufP, static_cast<void *>(d_reps), static_cast<void *>(d_dev),
+		for (void *p : {bufU, bufUnew, bufUt, bufP, static_cast<void *>(d_reps), static_cast<void *>(d_dev),
 		                static_cast<void *>(d_hist), static_cast<void *>(d_beta), static_cast<void *>(d_part),
 		                static_cast<void *>(d_res), static_cast<void *>(d_cnt)})
 			if (p)
@@ -508,13 +560,36 @@ struct mesh_batch_s
 		}
 		o.refresh(st, g_links, links, d_dev, red(K_OLD));
 		int last_p = n >= 3 ? n - 2 : -1;
+		bool flip = false; // the proposal is in Ut
+		auto unflip = [&] {
+			if (flip)
+			{
+				kb_swap_proposal<<<(R + 127) / 128, 128, 0, st>>>(d_reps, R);
+				MESH_LAUNCH_CHECK();
+				flip = false;
+			}
+		};
 		for (int i = 0; i < n; ++i)
 		{
 			if (i % 2 == 0)
+			{
+				unflip();
 				o.evolve(st, g_links, links, deltas[i], i == 0, i == n - 1);
+			}
+			else if (i + 1 < n)
+			{
+				// momentum step i fused with the link update i + 1
+				o.md(st, g_md, md_sp, d_beta, deltas[i], deltas[i + 1], flip, i + 1 == n - 1, red(K_NEW), i == last_p);
+				flip = !flip;
+				++i;
+			}
 			else
+			{
+				unflip();
 				o.force(st, g_force, force_sp, d_beta, deltas[i], red(K_NEW), i == last_p);
+			}
 		}
+		unflip();
 		o.plaquette(st, g_sites, sites, red(S_NEW), true);
 		kb_metropolis<<<(R + 127) / 128, 128, 0, st>>>(d_reps, R, d_dev, d_hist, hist_cap, d_beta, d_res + size_t(S_CUR) * R,
 		                                             d_res + size_t(K_OLD) * R, d_res + size_t(S_NEW) * R,
@@ -617,11 +692,13 @@ int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t
 		}
 		MESH_CUDA(cudaMalloc(&h->bufU, totU));
 		MESH_CUDA(cudaMalloc(&h->bufUnew, totU));
+		MESH_CUDA(cudaMalloc(&h->bufUt, totU));
 		MESH_CUDA(cudaMalloc(&h->bufP, totP));
 		for (int r = 0; r < nrep; ++r)
 		{
 			h->reps[r].U = static_cast<char *>(h->bufU) + offU[r];
 			h->reps[r].Unew = static_cast<char *>(h->bufUnew) + offU[r];
+			h->reps[r].Ut = static_cast<char *>(h->bufUt) + offU[r];
 			h->reps[r].P = static_cast<char *>(h->bufP) + offP[r];
 		}
 		MESH_CUDA(cudaMalloc(&h->d_reps, sizeof(BatchRep) * nrep));
@@ -636,7 +713,8 @@ int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t
 		h->force_sp =
 		    mesh_batch_s::make_space(h->d_reps, nrep, false, lch, sms * std::min(8, o.occupancy(1)), &h->g_force);
 		h->sites = mesh_batch_s::make_space(h->d_reps, nrep, true, sch, sms * std::min(8, o.occupancy(2)), &h->g_sites);
-		unsigned G = std::max({h->g_links, h->g_force, h->g_sites});
+		h->md_sp = mesh_batch_s::make_space(h->d_reps, nrep, true, sch, sms * std::min(8, o.occupancy(3)), &h->g_md);
+		unsigned G = std::max({h->g_links, h->g_force, h->g_sites, h->g_md});
 		MESH_CUDA(cudaMalloc(&h->d_part, sizeof(double) * size_t(G) * nrep));
 		MESH_CUDA(cudaMalloc(&h->d_res, sizeof(double) * 4 * size_t(nrep)));
 		MESH_CUDA(cudaMemset(h->d_res, 0, sizeof(double) * 4 * size_t(nrep)));
@@ -652,7 +730,7 @@ int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t
 	{
 		if (!h->ctx)
 		{
-			for (void *p : {h->bufU, h->bufUnew, h->bufP, static_cast<void *>(h->d_reps), static_cast<void *>(h->d_dev),
+			for (void *p : {h->bufU, h->bufUnew, h->bufUt, h->bufP, static_cast<void *>(h->d_reps), static_cast<void *>(h->d_dev),
 			                static_cast<void *>(h->d_beta), static_cast<void *>(h->d_part),
 			                static_cast<void *>(h->d_res), static_cast<void *>(h->d_cnt)})
 				if (p)
@@ -852,9 +930,11 @@ int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_del
 	return api_call([&] {
 		require(h != nullptr, "null batch");
 		require(n_deltas >= 1 && n_deltas % 2 == 1, "step table length must be odd");
-		// refresh + n MD steps + plaquette + Metropolis
+		// refresh + the first link update + (n - 1) / 2 fused MD steps (+ the
+		// pointer swap when that count is odd) + plaquette + Metropolis
+		int n_md = (n_deltas - 1) / 2;
 		if (launches_per_trajectory)
-			*launches_per_trajectory = n_deltas + 3;
+			*launches_per_trajectory = 1 + 1 + n_md + (n_md % 2) + 1 + 1;
 		if (grid_links)
 			*grid_links = int(h->g_force);
 		if (grid_sites)

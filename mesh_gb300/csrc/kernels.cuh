@@ -582,15 +582,127 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 // with the updated momentum (and project_on_group_fast when `reunit`), which
 // saves the separate link-update kernel's reads of U and P. The force of every
 // link reads U only, so writing Uout is race free.
-template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false>
-__global__ void __launch_bounds__(NT, MINB)
-    k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
-                         T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
+// The per-site body of the thread-per-site momentum step: the forces of the
+// ND links of site s, P_mu(s) -= coef F_mu and, with FUSE, the link update
+// Uout_mu(s) = exp(tu P_mu) U_mu(s); returns the kinetic norm of the updated
+// momenta. Shared by k_momentum_step_site and the batched replicas.
+template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD>
+__device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld,
+                                          T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	using Pr = Prod<GRP, T, F2>;
 	constexpr int NA = Gp::NA;
+	double acc = 0.0;
+	T F[ND][NA];
+#pragma unroll
+	for (int mu = 0; mu < ND; ++mu)
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			F[mu][a] = T(0);
+	// forward plaquette loops, one per plane
+#pragma unroll 1
+	for (int q = 0; q < ND * (ND - 1) / 2; ++q)
+	{
+		int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
+		E ab, dc;
+		if constexpr (ROWS)
+		{
+			// special unitary links: products from rows 0, 1 of the left factor
+			ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+			dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+		}
+		else
+		{
+			ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+			dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+		}
+		E pl = Pr::mul_nd(ab, dc);
+		T xa[NA];
+		Gp::proj(pl, xa);
+		add_plane<ND, NA>(F, q, xa);
+	}
+	// backward staples
+#pragma unroll 1
+	for (int mu = 0; mu < ND; ++mu)
+	{
+		E S = Gp::zero();
+#pragma unroll 1
+		for (int nu = 0; nu < ND; ++nu)
+		{
+			if (nu == mu)
+				continue;
+			int64_t y = eo_shift1<ND>(g, st, nu, -1);
+			E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
+			E ef;
+			if constexpr (ROWS)
+				ef = Pr::mul_r2(ld.rows(mu, y), f);
+			else
+				ef = Pr::mul(ld(mu, y), f);
+			Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
+		}
+		E W = Pr::mul(ld(mu, s), S);
+		T xa[NA];
+		Gp::proj(W, xa);
+		add_dir<ND, NA>(F, mu, xa);
+	}
+	if constexpr (!FUSE)
+	{
+#pragma unroll
+		for (int mu = 0; mu < ND; ++mu)
+		{
+			auto Pv = comp<T, NA>(P, g.V, mu);
+			T p[NA];
+			Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				p[a] -= coef * F[mu][a];
+			Pv.template store<CACHE_STREAM>(s, p);
+			acc += double(Gp::kin(p));
+		}
+	}
+	else
+	{
+		// one copy of the exp body: rolled direction loop
+#pragma unroll 1
+		for (int mu = 0; mu < ND; ++mu)
+		{
+			T f[NA];
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+			{
+				f[a] = F[0][a];
+#pragma unroll
+				for (int k = 1; k < ND; ++k)
+					f[a] = mu == k ? F[k][a] : f[a];
+			}
+			auto Pv = comp<T, NA>(P, g.V, mu);
+			T p[NA];
+			Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				p[a] -= coef * f[a];
+			Pv.template store<CACHE_STREAM>(s, p);
+			acc += double(Gp::kin(p));
+			E r;
+			if constexpr (ROWS)
+				r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
+			else
+				r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
+			if (reunit)
+				r = Gp::reunit_fast(r);
+			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
+		}
+	}
+	return acc;
+}
+
+template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false>
+__global__ void __launch_bounds__(NT, MINB)
+    k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
+                         T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
+{
 	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
 	double acc = 0.0;
 	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
@@ -601,106 +713,7 @@ __global__ void __launch_bounds__(NT, MINB)
 			tile_site<ND>(ts, tile, t, x);
 			Site<ND> st = site_from_coords<ND>(g, x);
 			int64_t s = eo_of<ND>(g, st);
-			T F[ND][NA];
-#pragma unroll
-			for (int mu = 0; mu < ND; ++mu)
-#pragma unroll
-				for (int a = 0; a < NA; ++a)
-					F[mu][a] = T(0);
-			// forward plaquette loops, one per plane
-#pragma unroll 1
-			for (int q = 0; q < ND * (ND - 1) / 2; ++q)
-			{
-				int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
-				E ab, dc;
-				if constexpr (ROWS)
-				{
-					// special unitary links: products from rows 0, 1 of the left factor
-					ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-					dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
-				}
-				else
-				{
-					ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-					dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
-				}
-				E pl = Pr::mul_nd(ab, dc);
-				T xa[NA];
-				Gp::proj(pl, xa);
-				add_plane<ND, NA>(F, q, xa);
-			}
-			// backward staples
-#pragma unroll 1
-			for (int mu = 0; mu < ND; ++mu)
-			{
-				E S = Gp::zero();
-#pragma unroll 1
-				for (int nu = 0; nu < ND; ++nu)
-				{
-					if (nu == mu)
-						continue;
-					int64_t y = eo_shift1<ND>(g, st, nu, -1);
-					E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
-					E ef;
-					if constexpr (ROWS)
-						ef = Pr::mul_r2(ld.rows(mu, y), f);
-					else
-						ef = Pr::mul(ld(mu, y), f);
-					Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
-				}
-				E W = Pr::mul(ld(mu, s), S);
-				T xa[NA];
-				Gp::proj(W, xa);
-				add_dir<ND, NA>(F, mu, xa);
-			}
-			if constexpr (!FUSE)
-			{
-#pragma unroll
-				for (int mu = 0; mu < ND; ++mu)
-				{
-					auto Pv = comp<T, NA>(P, g.V, mu);
-					T p[NA];
-					Pv.template load<CACHE_STREAM>(s, p);
-#pragma unroll
-					for (int a = 0; a < NA; ++a)
-						p[a] -= coef * F[mu][a];
-					Pv.template store<CACHE_STREAM>(s, p);
-					acc += double(Gp::kin(p));
-				}
-			}
-			else
-			{
-				// one copy of the exp body: rolled direction loop
-#pragma unroll 1
-				for (int mu = 0; mu < ND; ++mu)
-				{
-					T f[NA];
-#pragma unroll
-					for (int a = 0; a < NA; ++a)
-					{
-						f[a] = F[0][a];
-#pragma unroll
-						for (int k = 1; k < ND; ++k)
-							f[a] = mu == k ? F[k][a] : f[a];
-					}
-					auto Pv = comp<T, NA>(P, g.V, mu);
-					T p[NA];
-					Pv.template load<CACHE_STREAM>(s, p);
-#pragma unroll
-					for (int a = 0; a < NA; ++a)
-						p[a] -= coef * f[a];
-					Pv.template store<CACHE_STREAM>(s, p);
-					acc += double(Gp::kin(p));
-					E r;
-					if constexpr (ROWS)
-						r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
-					else
-						r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
-					if (reunit)
-						r = Gp::reunit_fast(r);
-					comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
-				}
-			}
+			acc += site_md<GRP, T, ND, F2, ROWS, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit);
 		}
 	}
 	if (kin.result)
