@@ -479,6 +479,7 @@ struct mesh_batch_s
 	BatchSpace links{}, sites{};
 	unsigned g_links = 0, g_force = 0, g_sites = 0, g_md = 0; // grids (links space uses g_links/g_force chunks)
 	BatchSpace md_sp{};
+	int use_md = -1; // fused MD steps (1) or separate kernels (0), timed at the first run; -1 not yet
 	BatchSpace force_sp{};
 	int64_t count = 0;
 	bool S_valid = false;
@@ -576,7 +577,7 @@ struct mesh_batch_s
 				unflip();
 				o.evolve(st, g_links, links, deltas[i], i == 0, i == n - 1);
 			}
-			else if (i + 1 < n)
+			else if (i + 1 < n && use_md == 1)
 			{
 				// momentum step i fused with the link update i + 1
 				o.md(st, g_md, md_sp, d_beta, deltas[i], deltas[i + 1], flip, i + 1 == n - 1, red(K_NEW), i == last_p);
@@ -596,6 +597,45 @@ struct mesh_batch_s
 		                                             d_res + size_t(K_NEW) * R, double(group_nc(group)));
 		MESH_LAUNCH_CHECK();
 		++count;
+	}
+
+	// fused or separate MD steps: whichever is faster on this batch, timed once
+	// (dp = du = 0: the momenta and the proposal keep their values; the first
+	// trajectory's momentum refresh and link update overwrite both anyway)
+	void tune_md()
+	{
+		if (use_md >= 0)
+			return;
+		cudaStream_t st = ctx->stream;
+		auto const &o = ops();
+		cudaEvent_t e0, e1;
+		MESH_CUDA(cudaEventCreate(&e0));
+		MESH_CUDA(cudaEventCreate(&e1));
+		auto timed = [&](auto &&f) {
+			f();
+			MESH_CUDA(cudaEventRecord(e0, st));
+			for (int r = 0; r < 3; ++r)
+				f();
+			MESH_CUDA(cudaEventRecord(e1, st));
+			MESH_CUDA(cudaEventSynchronize(e1));
+			float ms = 0;
+			MESH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+			return ms;
+		};
+		float t_md = timed([&] {
+			o.md(st, g_md, md_sp, d_beta, 0.0, 0.0, false, false, red(K_NEW), false);
+			o.md(st, g_md, md_sp, d_beta, 0.0, 0.0, true, false, red(K_NEW), false);
+		});
+		float t_sep = timed([&] {
+			for (int k = 0; k < 2; ++k)
+			{
+				o.force(st, g_force, force_sp, d_beta, 0.0, red(K_NEW), false);
+				o.evolve(st, g_links, links, 0.0, false, false);
+			}
+		});
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		use_md = t_md < t_sep ? 1 : 0;
 	}
 
 	// the replica's current link buffer (the descriptor table is updated on
@@ -824,6 +864,7 @@ int mesh_batch_run(mesh_batch h, double const *betas, double const *deltas, int 
 		// betas are read by the kernels from device memory: a captured
 		// trajectory stays valid when they change
 		MESH_CUDA(cudaMemcpyAsync(h->d_beta, betas, sizeof(double) * h->R, cudaMemcpyHostToDevice, st));
+		h->tune_md();
 		if (!use_graph)
 		{
 			for (int k = 0; k < count; ++k)
@@ -930,11 +971,12 @@ int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_del
 	return api_call([&] {
 		require(h != nullptr, "null batch");
 		require(n_deltas >= 1 && n_deltas % 2 == 1, "step table length must be odd");
-		// refresh + the first link update + (n - 1) / 2 fused MD steps (+ the
-		// pointer swap when that count is odd) + plaquette + Metropolis
+		// fused: refresh + the first link update + (n - 1) / 2 fused MD steps
+		// (+ the pointer swap when that count is odd) + plaquette + Metropolis;
+		// separate: refresh + n MD steps + plaquette + Metropolis
 		int n_md = (n_deltas - 1) / 2;
 		if (launches_per_trajectory)
-			*launches_per_trajectory = 1 + 1 + n_md + (n_md % 2) + 1 + 1;
+			*launches_per_trajectory = h->use_md == 1 ? 1 + 1 + n_md + (n_md % 2) + 1 + 1 : n_deltas + 3;
 		if (grid_links)
 			*grid_links = int(h->g_force);
 		if (grid_sites)

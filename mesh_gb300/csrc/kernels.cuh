@@ -1625,11 +1625,14 @@ template <int GRP, class T, int ND> struct Ops
 	// fastest thread-per-site variant of the fused step for this lattice, timed
 	// once with coef = 0 and tu = 0 (P unchanged, Uout = Uin); not while the
 	// stream is capturing
+	static constexpr int kSeparate = 1000; // the two steps as separate kernels were faster
 	static int choose_md(Field &P, Field const &Uin, Field &Uout)
 	{
 		int ov = force_override();
 		if (ov >= kMdFirst && ov <= kMdLast && force_variant_valid(Uin.geom, ov))
 			return ov;
+		if (ov >= 0 && ov < kMdFirst)
+			return kSeparate; // a thread-per-link variant pinned: no fusion
 		std::string key = "md_step/group" + std::to_string(GRP) + "/" + (sizeof(T) == 4 ? "f32" : "f64") + "/";
 		for (int i = 0; i < ND; ++i)
 			key += (i ? "x" : "") + std::to_string(Uin.dims[i]);
@@ -1672,9 +1675,35 @@ template <int GRP, class T, int ND> struct Ops
 				bestv = cand;
 			}
 		}
+		// against the momentum step and the link update as two kernels
+		{
+			int fv = choose_force(P, Uin, true);
+			auto pair = [&] {
+				launch_force(fv, P, Uin, T(0), RedSlot{}, true);
+				hmc_evolve(Uin, Uout, P, 0.0, false);
+			};
+			pair();
+			MESH_CUDA(cudaEventRecord(e0, c.stream));
+			for (int r = 0; r < 3; ++r)
+				pair();
+			MESH_CUDA(cudaEventRecord(e1, c.stream));
+			MESH_CUDA(cudaEventSynchronize(e1));
+			float ms = 0;
+			MESH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+			ms /= 3;
+			report += std::string(", separate ") + force_variant(fv).name + " + link update=" +
+			          std::to_string(ms * 1000.0f) + "us";
+			if (ms < best)
+			{
+				best = ms;
+				bestv = kSeparate;
+			}
+		}
 		cudaEventDestroy(e0);
 		cudaEventDestroy(e1);
-		set_tuned_variant(key, bestv, std::string("chosen ") + force_variant(bestv).name + " [" + report + "]");
+		set_tuned_variant(key, bestv,
+		                  std::string("chosen ") + (bestv == kSeparate ? "separate kernels" : force_variant(bestv).name) +
+		                      " [" + report + "]");
 		return bestv;
 	}
 	// momentum step P -= coef F(Uin) fused with the link update
@@ -1685,6 +1714,8 @@ template <int GRP, class T, int ND> struct Ops
 		if (!md_supported(Uin.geom))
 			return false;
 		int v = choose_md(P, Uin, Uout);
+		if (v == kSeparate)
+			return false;
 		launch_md(v, P, Uin, Uout, T(coef), T(tu), reunit ? 1 : 0, kin ? *kin : RedSlot{});
 		return true;
 	}
