@@ -285,9 +285,18 @@ class Field:
         _chk(load().mesh_field_import(self.h, a.ctypes.data_as(C.c_void_p), a.nbytes))
         return self
 
-    def export(self):
-        a = np.zeros(self._host_shape(), dtype=real_dtype(self.prec))
+    def export(self, out=None):
+        """the field in the reference's host layout; into `out` (a contiguous
+        array of the host shape, e.g. a view of pinned memory) when given"""
+        if out is None:
+            a = np.zeros(self._host_shape(), dtype=real_dtype(self.prec))
+        else:
+            a = out
+            assert a.flags["C_CONTIGUOUS"] and a.dtype == real_dtype(self.prec)
+            assert a.size == int(np.prod(self._host_shape())), "host array size does not match the field"
         _chk(load().mesh_field_export(self.h, a.ctypes.data_as(C.c_void_p), a.nbytes))
+        if out is not None:
+            return out
         return a if self.nstack > 1 else a[0]
 
     def copy_from(self, other: "Field"):

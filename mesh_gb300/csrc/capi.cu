@@ -125,12 +125,34 @@ void same_shape(Field const &a, Field const &b)
 
 double nplanes(int nd) { return nd * (nd - 1) * 0.5; }
 
+// the device address of a pinned (page-locked, mapped) host buffer that a
+// kernel may read and write directly, 16-byte aligned; nullptr otherwise
+// (pageable memory goes through a staging copy)
+static void *mapped_host(void const *host)
+{
+	if (reinterpret_cast<uintptr_t>(host) % 16 != 0)
+		return nullptr;
+	cudaPointerAttributes a{};
+	if (cudaPointerGetAttributes(&a, host) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return nullptr;
+	}
+	return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 void import_host(Field &f, void const *host, size_t bytes)
 {
 	require(host != nullptr, "null host buffer");
 	require(bytes == f.host_bytes(), "host buffer size does not match the field");
 	auto &c = *f.ctx;
 	DeviceGuard dg(c.device);
+	if (void *d = mapped_host(host))
+	{
+		ops_for(f).import_direct(f, d);
+		MESH_CUDA(cudaStreamSynchronize(c.stream));
+		return;
+	}
 	void *stage = c.stage(bytes);
 	MESH_CUDA(cudaMemcpyAsync(stage, host, bytes, cudaMemcpyHostToDevice, c.stream));
 	ops_for(f).import_(f, stage);
@@ -143,6 +165,12 @@ void export_host(Field const &f, void *host, size_t bytes)
 	require(bytes == f.host_bytes(), "host buffer size does not match the field");
 	auto &c = *f.ctx;
 	DeviceGuard dg(c.device);
+	if (void *d = mapped_host(host))
+	{
+		ops_for(f).export_direct(f, d);
+		MESH_CUDA(cudaStreamSynchronize(c.stream));
+		return;
+	}
 	void *stage = c.stage(bytes);
 	ops_for(f).export_(f, stage);
 	MESH_CUDA(cudaMemcpyAsync(host, stage, bytes, cudaMemcpyDeviceToHost, c.stream));

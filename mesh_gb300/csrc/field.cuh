@@ -124,6 +124,9 @@ struct OpsTable
 	void (*wilson_rt)(Field const &U, int r, int t, void const *S, void const *Tt, RedSlot out);
 	// one heat-bath (overrelax = false) or overrelaxation sweep, checkerboard order
 	void (*gauge_sweep)(Field &U, double beta, uint64_t seed, uint64_t ctr, bool overrelax);
+	// layout conversion reading / writing a device-accessible host buffer directly
+	void (*import_direct)(Field &f, void const *host);
+	void (*export_direct)(Field const &f, void *host);
 };
 
 // autotuning registry (tune.cu): variant index per kernel/lattice key

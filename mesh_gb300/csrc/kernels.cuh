@@ -102,6 +102,133 @@ __global__ void __launch_bounds__(kBlock) k_export(Geom g, int nstack, T const *
 	}
 }
 
+// Direct host transfers: the host buffer is mapped into the device's address
+// space (pinned memory), so the conversion kernel reads or writes it over the
+// host link itself, without a staging copy. A block moves kBlock consecutive
+// host objects of one component as contiguous 16-byte words through shared
+// memory (the host side stays coalesced) and the threads scatter them to (or
+// gather them from) the even/odd device layout. The host buffer must be
+// 16-byte aligned.
+template <int ND> __device__ __forceinline__ int64_t eo_of_lex(Geom const &g, int64_t lex)
+{
+	uint32_t r = uint32_t(lex);
+	int sum = 0;
+#pragma unroll
+	for (int i = ND - 1; i >= 0; --i)
+	{
+		uint32_t L = uint32_t(g.L[i]);
+		uint32_t q = uint32_t((uint64_t(r) * g.dm[i]) >> g.ds[i]);
+		sum += int(r - q * L);
+		r = q;
+	}
+	return int64_t(sum & 1) * g.Vh + (lex >> 1);
+}
+
+template <int GRP, class T, int ND, bool ALG>
+__global__ void __launch_bounds__(kBlock)
+    k_import_direct(Geom g, int nstack, T const *__restrict__ host, T *__restrict__ dev)
+{
+	using Gp = Group<GRP, T>;
+	constexpr int NRH = Gp::NR;
+	constexpr int NR = ALG ? Gp::NA : Gp::NR;
+	__shared__ __align__(16) T tile[kBlock * NRH];
+	int64_t bpc = (g.V + kBlock - 1) / kBlock; // blocks per component
+	for (int64_t b = blockIdx.x; b < int64_t(nstack) * bpc; b += gridDim.x)
+	{
+		int c = int(b / bpc);
+		int64_t lex0 = (b - int64_t(c) * bpc) * kBlock;
+		int cnt = int(g.V - lex0 < kBlock ? g.V - lex0 : kBlock);
+		T const *src = host + (int64_t(c) * g.V + lex0) * NRH;
+		int nreal = cnt * NRH;
+		int nvec = int((size_t(nreal) * sizeof(T)) / 16);
+		constexpr int PER = 16 / sizeof(T);
+		__syncthreads();
+		for (int k = threadIdx.x; k < nvec; k += kBlock)
+			reinterpret_cast<uint4 *>(tile)[k] = __ldcs(reinterpret_cast<uint4 const *>(src) + k);
+		for (int k = nvec * PER + threadIdx.x; k < nreal; k += kBlock)
+			tile[k] = src[k];
+		__syncthreads();
+		if (threadIdx.x < cnt)
+		{
+			int64_t lex = lex0 + threadIdx.x;
+			T const *o = tile + threadIdx.x * NRH;
+			T v[NR];
+			if constexpr (!ALG)
+			{
+#pragma unroll
+				for (int k = 0; k < NR; ++k)
+					v[k] = o[k];
+			}
+			else if constexpr (GRP == U1)
+				v[0] = o[1];
+			else if constexpr (GRP == SU2)
+			{
+				v[0] = o[1];
+				v[1] = o[2];
+				v[2] = o[3];
+			}
+			else
+			{
+				v[0] = o[1];
+				v[1] = o[9];
+				v[2] = o[2];
+				v[3] = o[3];
+				v[4] = o[4];
+				v[5] = o[5];
+				v[6] = o[10];
+				v[7] = o[11];
+			}
+			comp<T, NR>(dev, g.V, c).store(eo_of_lex<ND>(g, lex), v);
+		}
+	}
+}
+
+template <int GRP, class T, int ND, bool ALG>
+__global__ void __launch_bounds__(kBlock)
+    k_export_direct(Geom g, int nstack, T const *__restrict__ dev, T *__restrict__ host)
+{
+	using Gp = Group<GRP, T>;
+	constexpr int NRH = Gp::NR;
+	constexpr int NR = ALG ? Gp::NA : Gp::NR;
+	__shared__ __align__(16) T tile[kBlock * NRH];
+	int64_t bpc = (g.V + kBlock - 1) / kBlock;
+	for (int64_t b = blockIdx.x; b < int64_t(nstack) * bpc; b += gridDim.x)
+	{
+		int c = int(b / bpc);
+		int64_t lex0 = (b - int64_t(c) * bpc) * kBlock;
+		int cnt = int(g.V - lex0 < kBlock ? g.V - lex0 : kBlock);
+		__syncthreads();
+		if (threadIdx.x < cnt)
+		{
+			T v[NR];
+			comp<T, NR>(const_cast<T *>(dev), g.V, c).load(eo_of_lex<ND>(g, lex0 + threadIdx.x), v);
+			T *o = tile + threadIdx.x * NRH;
+			if constexpr (!ALG)
+			{
+#pragma unroll
+				for (int k = 0; k < NR; ++k)
+					o[k] = v[k];
+			}
+			else
+			{
+				typename Gp::E e = Gp::from_alg(v);
+#pragma unroll
+				for (int k = 0; k < NRH; ++k)
+					o[k] = e.v[k];
+			}
+		}
+		__syncthreads();
+		T *dst = host + (int64_t(c) * g.V + lex0) * NRH;
+		int nreal = cnt * NRH;
+		int nvec = int((size_t(nreal) * sizeof(T)) / 16);
+		constexpr int PER = 16 / sizeof(T);
+		for (int k = threadIdx.x; k < nvec; k += kBlock)
+			__stcs(reinterpret_cast<uint4 *>(dst) + k, reinterpret_cast<uint4 const *>(tile)[k]);
+		for (int k = nvec * PER + threadIdx.x; k < nreal; k += kBlock)
+			dst[k] = tile[k];
+	}
+}
+
 // ---------------------------------------------------------------------------
 // initialisation and random fields
 // ---------------------------------------------------------------------------
@@ -1239,6 +1366,33 @@ template <int GRP, class T, int ND> struct Ops
 			                                                                    static_cast<T *>(f.d));
 		MESH_LAUNCH_CHECK();
 	}
+	// conversion straight from / to a device-accessible host buffer
+	static void import_direct(Field &f, void const *host)
+	{
+		auto &c = *f.ctx;
+		int64_t nb = int64_t(f.nstack) * ((f.geom.V + kBlock - 1) / kBlock);
+		unsigned b = unsigned(nb < int64_t(c.num_sms) * 8 ? nb : int64_t(c.num_sms) * 8);
+		if (f.kind == MESH_GROUP)
+			k_import_direct<GRP, T, ND, false><<<b, kBlock, 0, c.stream>>>(f.geom, f.nstack, static_cast<T const *>(host),
+			                                                               static_cast<T *>(f.d));
+		else
+			k_import_direct<GRP, T, ND, true><<<b, kBlock, 0, c.stream>>>(f.geom, f.nstack, static_cast<T const *>(host),
+			                                                              static_cast<T *>(f.d));
+		MESH_LAUNCH_CHECK();
+	}
+	static void export_direct(Field const &f, void *host)
+	{
+		auto &c = *f.ctx;
+		int64_t nb = int64_t(f.nstack) * ((f.geom.V + kBlock - 1) / kBlock);
+		unsigned b = unsigned(nb < int64_t(c.num_sms) * 8 ? nb : int64_t(c.num_sms) * 8);
+		if (f.kind == MESH_GROUP)
+			k_export_direct<GRP, T, ND, false><<<b, kBlock, 0, c.stream>>>(f.geom, f.nstack, static_cast<T const *>(f.d),
+			                                                               static_cast<T *>(host));
+		else
+			k_export_direct<GRP, T, ND, true><<<b, kBlock, 0, c.stream>>>(f.geom, f.nstack, static_cast<T const *>(f.d),
+			                                                              static_cast<T *>(host));
+		MESH_LAUNCH_CHECK();
+	}
 	static void export_(Field const &f, void *stage)
 	{
 		auto &c = *f.ctx;
@@ -1900,7 +2054,7 @@ template <int GRP, class T, int ND> struct Ops
 		                           exp_apply,    axpy_alg,      gauge_transform, tune,
 		                           hmc_plaquette, hmc_evolve,   hmc_momentum_step, hmc_tune,
 		                           hmc_md_step,   hmc_tune_md,  line_extend,    wilson_rt,
-		                           gauge_sweep};
+		                           gauge_sweep,   import_direct, export_direct};
 		return &t;
 	}
 };

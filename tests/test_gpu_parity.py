@@ -308,6 +308,30 @@ def test_run_host_roundtrip(ctx, oracle):
     assert rel(host, h.U.export()) == 0.0
 
 
+@pytest.mark.parametrize("dims", [[4, 6, 4, 8], [4, 6, 2, 6]])
+@pytest.mark.parametrize("g,p", CASES)
+def test_pinned_host_transfers_match_staged(ctx, oracle, g, p, dims):
+    """gauge fields and momenta through pinned host buffers (converted by the
+    kernels that read and write the mapped host memory directly, 256 objects
+    per block; V = 768 and V = 288, a partial last block) equal the path
+    through a staging copy, bit for bit"""
+    torch = pytest.importorskip("torch")
+    dt = mg.real_dtype(p)
+    tdt = torch.float64 if p == 2 else torch.float32
+    U64 = thermal(oracle, g, dims)
+    P64 = oracle.random_momenta(g, 2, dims, 9, 0)
+    for arr, ctor in ((U64, mg.GaugeField), (P64, mg.Momenta)):
+        host = arr.astype(dt)
+        pin = torch.empty(host.shape, dtype=tdt, pin_memory=True)
+        pin.numpy()[...] = host
+        F = ctor(ctx, g, p, mg.Grid(dims)).import_(pin.numpy())
+        staged = F.export()
+        assert np.array_equal(staged, host)
+        out = torch.zeros(host.shape, dtype=tdt, pin_memory=True)
+        F.export(out.numpy())
+        assert np.array_equal(out.numpy(), host)
+
+
 @pytest.mark.parametrize("variant", [-1, 11, 13, 14, 15, 16, 17, 18, 20, 21, 22, 23, 24, 25, 26])
 @pytest.mark.parametrize("g", [2, 3])
 def test_trajectory_momentum_step_matches_generic(ctx, oracle, g, variant):
