@@ -1568,8 +1568,9 @@ template <int GRP, class T, int ND> struct Ops
 	// (k_momentum_step_site) with FP32x2 products; 18-20: thread per site,
 	// plain products; 23-24: thread per site, FP32x2, whole links read (no
 	// row rebuilt: fewer products, more bytes through L1); 25-26: thread per
-	// site, FP32x2 with the second pairing (broadcast left factor)
-	static constexpr int kForceVariants = 27;
+	// site, FP32x2 with the second pairing (broadcast left factor); 27-32:
+	// thread per site, FP32x2, 128 threads x 4 blocks, other tile shapes
+	static constexpr int kForceVariants = 33;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1600,7 +1601,13 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/full", true, true},
 		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2/full", true, true},
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2b", 2},
-		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2}};
+		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2},
+		    {2, {0, 1, 3, 3}, 128, 4, "site/tile1x2x8x8/128thr/4blk/f32x2", 1},
+		    {2, {1, 2, 2, 2}, 128, 4, "site/tile2x4x4x4/128thr/4blk/f32x2", 1},
+		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/f32x2", 1},
+		    {2, {2, 1, 1, 3}, 128, 4, "site/tile4x2x2x8/128thr/4blk/f32x2", 1},
+		    {2, {0, 0, 3, 4}, 128, 4, "site/tile1x1x8x16/128thr/4blk/f32x2", 1},
+		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1732,7 +1739,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
-	static constexpr int kMdFirst = 14, kMdLast = 26; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 32; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4 || sizeof(T) != 4)

@@ -191,7 +191,7 @@ def test_su3_exp_fp32_series_and_closed_form(ctx, oracle, t):
     assert rel(U.export(), oracle.evolve(3, 2, dims, U64, P64, t)) < TOL32
 
 
-@pytest.mark.parametrize("variant", list(range(27)))
+@pytest.mark.parametrize("variant", list(range(33)))
 @pytest.mark.parametrize("g,p", [(3, 1), (3, 2), (2, 1), (1, 1)])
 def test_every_force_launch_variant_vs_oracle(ctx, oracle, g, p, variant):
     """each launch variant the autotuner can choose (thread per link in
@@ -383,7 +383,7 @@ def test_md_step_vs_oracle(ctx, oracle, g, p):
     assert rel(h.U.export(), U_o) < 2 * tol(p)
 
 
-MD_VARIANTS = [(3, v) for v in (-1, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26)] + [(g, v) for g in (1, 2) for v in (-1, 18, 20)]
+MD_VARIANTS = [(3, v) for v in (-1, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 32)] + [(g, v) for g in (1, 2) for v in (-1, 18, 20)]
 
 
 @pytest.mark.parametrize("g,variant", MD_VARIANTS)
