@@ -32,6 +32,15 @@ template <class T> struct cx
 {
 	T re, im;
 };
+
+// cos x and sin(x)/x from x^2 for x^2 < 1/4 by their Taylor series through
+// x^8 (remainders below x^10/10! < 3e-10): the small angles of FP32 link
+// updates, without a range-reduced sincos
+template <class T> MESH_HD void cos_sinc_small(T x2, T *c, T *sc)
+{
+	*c = T(1) - x2 * (T(1.0 / 2) - x2 * (T(1.0 / 24) - x2 * (T(1.0 / 720) - x2 * T(1.0 / 40320))));
+	*sc = T(1) - x2 * (T(1.0 / 6) - x2 * (T(1.0 / 120) - x2 * (T(1.0 / 5040) - x2 * T(1.0 / 362880))));
+}
 template <class T> MESH_HD cx<T> cmul(cx<T> a, cx<T> b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
 template <class T> MESH_HD cx<T> cadd(cx<T> a, cx<T> b) { return {a.re + b.re, a.im + b.im}; }
 template <class T> MESH_HD cx<T> csub(cx<T> a, cx<T> b) { return {a.re - b.re, a.im - b.im}; }
@@ -98,8 +107,16 @@ template <class T> struct Group<U1, T>
 	// exp(t X)
 	MESH_HD static E exp_alg(T const *o, T t)
 	{
+		T x = o[0] * t;
+		if constexpr (sizeof(T) == 4)
+			if (x * x < T(0.25))
+			{
+				T c, sc;
+				cos_sinc_small(x * x, &c, &sc);
+				return {{c, x * sc}};
+			}
 		T s, c;
-		m_sincos(o[0] * t, &s, &c);
+		m_sincos(x, &s, &c);
 		return {{c, s}};
 	}
 	MESH_HD static E reunit_fast(E a)
@@ -176,6 +193,16 @@ template <class T> struct Group<SU2, T>
 	MESH_HD static E exp_alg(T const *o, T t)
 	{
 		T a1 = o[0] * t, a2 = o[1] * t, a3 = o[2] * t;
+		if constexpr (sizeof(T) == 4)
+		{
+			T al2 = a1 * a1 + a2 * a2 + a3 * a3;
+			if (al2 < T(0.25))
+			{
+				T c, sc;
+				cos_sinc_small(al2, &c, &sc);
+				return {{c, a1 * sc, a2 * sc, a3 * sc}};
+			}
+		}
 		T al = m_sqrt(a1 * a1 + a2 * a2 + a3 * a3);
 		T s, c;
 		m_sincos(al, &s, &c);

@@ -178,17 +178,20 @@ def test_staples_force_evolve_reunit_vs_oracle(ctx, oracle, g, p):
 
 
 @pytest.mark.parametrize("t", [0.01, 0.05, 0.2, 0.6, 2.0])
-def test_su3_exp_fp32_series_and_closed_form(ctx, oracle, t):
-    """FP32 SU(3) link update exp(t P) U: for |t P| < 1 the truncated power
-    series with the Cayley-Hamilton reduction, above it the closed form; both
-    against the FP64 oracle (Taylor with scaling and squaring)"""
+@pytest.mark.parametrize("g", [1, 2, 3])
+def test_exp_fp32_series_and_closed_form(ctx, oracle, g, t):
+    """FP32 link update exp(t P) U: small arguments by truncated series (SU(3):
+    the power series reduced by Cayley-Hamilton for |t P| < 1; U(1), SU(2):
+    the Taylor series of cos and sin(x)/x for |x| < 1/2), larger ones by the
+    closed forms; against the FP64 oracle (groups.h exp; SU(3) Taylor with
+    scaling and squaring)"""
     dims = [4, 4, 4, 8]
-    U64 = thermal(oracle, 3, dims)
-    P64 = oracle.random_momenta(3, 2, dims, 9, 0)
-    U = gauge(ctx, 3, 1, dims, U64.astype(np.float32))
-    P = momenta(ctx, 3, 1, dims, P64.astype(np.float32))
+    U64 = thermal(oracle, g, dims)
+    P64 = oracle.random_momenta(g, 2, dims, 9, 0)
+    U = gauge(ctx, g, 1, dims, U64.astype(np.float32))
+    P = momenta(ctx, g, 1, dims, P64.astype(np.float32))
     mg.evolve(U, P, t)
-    assert rel(U.export(), oracle.evolve(3, 2, dims, U64, P64, t)) < TOL32
+    assert rel(U.export(), oracle.evolve(g, 2, dims, U64, P64, t)) < TOL32
 
 
 @pytest.mark.parametrize("variant", list(range(33)))
