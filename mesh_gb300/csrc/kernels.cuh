@@ -1738,11 +1738,11 @@ template <int GRP, class T, int ND> struct Ops
 		b = unsigned(ts.ntiles < cap ? ts.ntiles : cap);
 		return ts;
 	}
-	// ---- fused momentum step + link update (trajectory, FP32 links) ---------
+	// ---- fused momentum step + link update (trajectory) ----------------------
 	static constexpr int kMdFirst = 14, kMdLast = 32; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
-		if constexpr (ND != 4 || sizeof(T) != 4)
+		if constexpr (ND != 4)
 			return false;
 		for (int v = kMdFirst; v <= kMdLast; ++v)
 			if (force_variant_valid(g, v))
