@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kChunk)
 		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
 		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true>(rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
 		                                                          static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
-		                                                          reunit);
+		                                                          reunit, KIN);
 		return KIN ? k : 0.0;
 	});
 }

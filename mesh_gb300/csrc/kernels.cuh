@@ -567,7 +567,9 @@ __global__ void __launch_bounds__(NT, MINB)
 		int mu = int(i / g.V);
 		int64_t s = i - int64_t(mu) * g.V;
 		Site<ND> st = site_from_eo<ND>(g, s);
-		acc += force_item<GRP, T, ND>(g, st, s, mu, ld, P, coef);
+		double k = force_item<GRP, T, ND>(g, st, s, mu, ld, P, coef);
+		if (kin.result)
+			acc += k;
 	}
 	if (kin.result)
 		grid_sum<NT>(acc, kin);
@@ -615,7 +617,11 @@ __global__ void __launch_bounds__(NT, MINB)
 			int64_t s = eo_of<ND>(g, st);
 #pragma unroll 1
 			for (int mu = 0; mu < ND; ++mu)
-				acc += force_item<GRP, T, ND, F2>(g, st, s, mu, ld, P, coef);
+			{
+				double k = force_item<GRP, T, ND, F2>(g, st, s, mu, ld, P, coef);
+				if (kin.result)
+					acc += k;
+			}
 		}
 	}
 	if (kin.result)
@@ -712,10 +718,13 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 // The per-site body of the thread-per-site momentum step: the forces of the
 // ND links of site s, P_mu(s) -= coef F_mu and, with FUSE, the link update
 // Uout_mu(s) = exp(tu P_mu) U_mu(s); returns the kinetic norm of the updated
-// momenta. Shared by k_momentum_step_site and the batched replicas.
+// momenta when want_kin (the FP64 sum costs FP64-pipe time: only the last
+// momentum step of a trajectory asks for it). Shared by k_momentum_step_site
+// and the batched replicas.
 template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD>
 __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld,
-                                          T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit)
+                                          T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
+                                          bool want_kin)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
@@ -786,7 +795,8 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			for (int a = 0; a < NA; ++a)
 				p[a] -= coef * F[mu][a];
 			Pv.template store<CACHE_STREAM>(s, p);
-			acc += double(Gp::kin(p));
+			if (want_kin)
+				acc += double(Gp::kin(p));
 		}
 	}
 	else
@@ -811,7 +821,8 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			for (int a = 0; a < NA; ++a)
 				p[a] -= coef * f[a];
 			Pv.template store<CACHE_STREAM>(s, p);
-			acc += double(Gp::kin(p));
+			if (want_kin)
+				acc += double(Gp::kin(p));
 			E r;
 			if constexpr (ROWS)
 				r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
@@ -840,7 +851,7 @@ __global__ void __launch_bounds__(NT, MINB)
 			tile_site<ND>(ts, tile, t, x);
 			Site<ND> st = site_from_coords<ND>(g, x);
 			int64_t s = eo_of<ND>(g, st);
-			acc += site_md<GRP, T, ND, F2, ROWS, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit);
+			acc += site_md<GRP, T, ND, F2, ROWS, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit, kin.result != nullptr);
 		}
 	}
 	if (kin.result)
