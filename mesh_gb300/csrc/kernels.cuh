@@ -584,27 +584,7 @@ struct TileSpec
 	int nt[4];
 	int sites;  // sites per tile
 	int ntiles; // tiles in the lattice
-	// 0: blocks take tiles grid-stride in lexicographic tile order; 1
-	// (marching): tiles ordered with dimension 0 fastest and each block takes
-	// a contiguous range, so a block's consecutive tiles are neighbours in
-	// dimension 0 and the shared face of the previous tile is still in L1
-	int march;
 };
-
-// the tiles of block b: [first, end) with step
-struct TileRange
-{
-	int first, end, step;
-};
-__device__ __forceinline__ TileRange tile_range(TileSpec const &ts)
-{
-	if (ts.march)
-	{
-		int64_t G = gridDim.x, b = blockIdx.x;
-		return {int(b * ts.ntiles / G), int((b + 1) * ts.ntiles / G), 1};
-	}
-	return {int(blockIdx.x), ts.ntiles, int(gridDim.x)};
-}
 
 template <int GRP, class T, int ND, int NT, int MINB, bool F2 = false, bool ROWS = false>
 __global__ void __launch_bounds__(NT, MINB)
@@ -652,33 +632,14 @@ __global__ void __launch_bounds__(NT, MINB)
 // lexicographic with the last dimension fastest)
 template <int ND> __device__ __forceinline__ void tile_site(TileSpec const &ts, int tile, int t, int *x)
 {
-	int tc[ND];
 	int r = tile;
-	if (ts.march)
-	{
-#pragma unroll
-		for (int i = 0; i < ND; ++i)
-		{
-			int q = r / ts.nt[i];
-			tc[i] = r - q * ts.nt[i];
-			r = q;
-		}
-	}
-	else
-	{
-#pragma unroll
-		for (int i = ND - 1; i >= 0; --i)
-		{
-			int q = r / ts.nt[i];
-			tc[i] = r - q * ts.nt[i];
-			r = q;
-		}
-	}
 #pragma unroll
 	for (int i = ND - 1; i >= 0; --i)
 	{
-		x[i] = (tc[i] << ts.lt[i]) + (t & ((1 << ts.lt[i]) - 1));
+		int q = r / ts.nt[i];
+		x[i] = ((r - q * ts.nt[i]) << ts.lt[i]) + (t & ((1 << ts.lt[i]) - 1));
 		t >>= ts.lt[i];
+		r = q;
 	}
 }
 
@@ -882,8 +843,7 @@ __global__ void __launch_bounds__(NT, MINB)
 {
 	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
 	double acc = 0.0;
-	TileRange tr = tile_range(ts);
-	for (int tile = tr.first; tile < tr.end; tile += tr.step)
+	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
 	{
 		for (int t = threadIdx.x; t < ts.sites; t += NT)
 		{
@@ -1612,7 +1572,6 @@ template <int GRP, class T, int ND> struct Ops
 		char const *name;
 		int f2 = 0;        // packed FP32x2 products, pairing 1 or 2 (SU(3) float only)
 		bool full = false; // read all 18 reals of SU(3) FP32 links even where rows 0, 1 would do
-		bool march = false; // blocks march through contiguous tile ranges along dimension 0
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1621,9 +1580,8 @@ template <int GRP, class T, int ND> struct Ops
 	// plain products; 23-24: thread per site, FP32x2, whole links read (no
 	// row rebuilt: fewer products, more bytes through L1); 25-26: thread per
 	// site, FP32x2 with the second pairing (broadcast left factor); 27-32:
-	// thread per site, FP32x2, 128 threads x 4 blocks, other tile shapes;
-	// 33-35: the same, blocks marching along dimension 0
-	static constexpr int kForceVariants = 36;
+	// thread per site, FP32x2, 128 threads x 4 blocks, other tile shapes
+	static constexpr int kForceVariants = 33;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1660,10 +1618,7 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/f32x2", 1},
 		    {2, {2, 1, 1, 3}, 128, 4, "site/tile4x2x2x8/128thr/4blk/f32x2", 1},
 		    {2, {0, 0, 3, 4}, 128, 4, "site/tile1x1x8x16/128thr/4blk/f32x2", 1},
-		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1},
-		    {2, {0, 2, 2, 3}, 128, 4, "site/march/tile1x4x4x8/128thr/4blk/f32x2", 1, false, true},
-		    {2, {0, 1, 3, 3}, 128, 4, "site/march/tile1x2x8x8/128thr/4blk/f32x2", 1, false, true},
-		    {2, {1, 1, 2, 3}, 128, 4, "site/march/tile2x2x4x8/128thr/4blk/f32x2", 1, false, true}};
+		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1792,11 +1747,10 @@ template <int GRP, class T, int ND> struct Ops
 		}
 		int64_t cap = int64_t(c.num_sms) * fv.minb;
 		b = unsigned(ts.ntiles < cap ? ts.ntiles : cap);
-		ts.march = fv.march ? 1 : 0;
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 35; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 32; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
