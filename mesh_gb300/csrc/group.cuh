@@ -717,7 +717,7 @@ template <class T> struct Group<SU3, T>
 //   (cr, ci) += (ar, ai) * (br, br);  (cr, ci) += (-ai, ar) * (bi, bi),
 // halving the FMA instruction count of the 3x3 products.
 // ---------------------------------------------------------------------------
-template <int FORM> struct Su3F2T
+struct Su3F2
 {
 	using E = Group<SU3, float>::E;
 	__device__ __forceinline__ static unsigned long long pk(float a, float b)
@@ -738,77 +738,38 @@ template <int FORM> struct Su3F2T
 		return d;
 	}
 	// generic product with operand access functors: c_ij = sum_k A(i,k) B(k,j)
-	// for the rows i < NRW, where A(i,k) = (ar, ai) and B(k,j) = (br, bi).
-	// FORM 1: the pairs are (re, im) of A against broadcast parts of B:
-	//   (cr, ci) += (ar, ai) * (br, br) + (-ai, ar) * (bi, bi);
-	// FORM 2: broadcast parts of A against the (re, im) pairs of B:
-	//   (cr, ci) += (ar, ar) * (br, bi) + (ai, ai) * (-bi, br).
+	// for the rows i < NRW, where A(i,k) = (ar, ai) and B(k,j) = (br, bi):
+	//   (cr, ci) += (ar, ai) * (br, br) + (-ai, ar) * (bi, bi)
+	// (pairing the other way round, broadcast parts of A against (re, im)
+	// pairs of B, measured slower)
 	template <int NRW, class FA, class FB> __device__ __forceinline__ static E prod(FA fa, FB fb)
 	{
 		E r;
-		if constexpr (FORM == 1)
+#pragma unroll
+		for (int i = 0; i < NRW; ++i)
 		{
-#pragma unroll
-			for (int i = 0; i < NRW; ++i)
-			{
-				unsigned long long an[3], ar[3];
-#pragma unroll
-				for (int k = 0; k < 3; ++k)
-				{
-					float re, im;
-					fa(i, k, re, im);
-					an[k] = pk(re, im);
-					ar[k] = pk(-im, re);
-				}
-#pragma unroll
-				for (int j = 0; j < 3; ++j)
-				{
-					unsigned long long acc = 0ull;
-#pragma unroll
-					for (int k = 0; k < 3; ++k)
-					{
-						float re, im;
-						fb(k, j, re, im);
-						acc = fma2(an[k], pk(re, re), acc);
-						acc = fma2(ar[k], pk(im, im), acc);
-					}
-					upk(acc, r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
-				}
-			}
-		}
-		else
-		{
-			unsigned long long bn[3][3], bs[3][3];
+			unsigned long long an[3], ar[3];
 #pragma unroll
 			for (int k = 0; k < 3; ++k)
+			{
+				float re, im;
+				fa(i, k, re, im);
+				an[k] = pk(re, im);
+				ar[k] = pk(-im, re);
+			}
 #pragma unroll
-				for (int j = 0; j < 3; ++j)
+			for (int j = 0; j < 3; ++j)
+			{
+				unsigned long long acc = 0ull;
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
 				{
 					float re, im;
 					fb(k, j, re, im);
-					bn[k][j] = pk(re, im);
-					bs[k][j] = pk(-im, re);
+					acc = fma2(an[k], pk(re, re), acc);
+					acc = fma2(ar[k], pk(im, im), acc);
 				}
-#pragma unroll
-			for (int i = 0; i < NRW; ++i)
-			{
-				unsigned long long acc[3] = {0ull, 0ull, 0ull};
-#pragma unroll
-				for (int k = 0; k < 3; ++k)
-				{
-					float re, im;
-					fa(i, k, re, im);
-					unsigned long long rr = pk(re, re), ii = pk(im, im);
-#pragma unroll
-					for (int j = 0; j < 3; ++j)
-					{
-						acc[j] = fma2(rr, bn[k][j], acc[j]);
-						acc[j] = fma2(ii, bs[k][j], acc[j]);
-					}
-				}
-#pragma unroll
-				for (int j = 0; j < 3; ++j)
-					upk(acc[j], r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
+				upk(acc, r.v[6 * i + 2 * j], r.v[6 * i + 2 * j + 1]);
 			}
 		}
 		return r;
@@ -834,6 +795,6 @@ template <int FORM> struct Su3F2T
 		    [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
 	}
 };
-using Su3F2 = Su3F2T<1>;
+
 
 } // namespace meshgb

@@ -457,8 +457,7 @@ __global__ void __launch_bounds__(kBlock) k_plaquette(Geom g, T const *__restric
 	grid_sum<kBlock>(acc, out);
 }
 
-// 3x3 products of the force: packed FP32x2 FMAs for SU(3) float when F2 > 0
-// (F2 = 1 or 2: the two pairings of Su3F2T). mul_r2: the product of two
+// 3x3 products of the force: packed FP32x2 FMAs for SU(3) float when F2 = 1. mul_r2: the product of two
 // special unitary matrices from rows 0 and 1 of the left one (row 2 of the
 // result rebuilt); the plain product for the other groups.
 template <int GRP, class T, int F2> struct Prod
@@ -476,10 +475,10 @@ template <int GRP, class T, int F2> struct Prod
 			return Gp::mul(a, b);
 	}
 };
-template <int F2> struct ProdF2
+struct ProdF2
 {
 	using E = Group<SU3, float>::E;
-	using S = Su3F2T<F2>;
+	using S = Su3F2;
 	__device__ __forceinline__ static E mul(E const &a, E const &b) { return S::template mul<3>(a, b); }
 	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return S::mul_nd(a, b); }
 	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return S::mul_dn(a, b); }
@@ -490,10 +489,7 @@ template <int F2> struct ProdF2
 		return r;
 	}
 };
-template <> struct Prod<SU3, float, 1> : ProdF2<1>
-{
-};
-template <> struct Prod<SU3, float, 2> : ProdF2<2>
+template <> struct Prod<SU3, float, 1> : ProdF2
 {
 };
 
@@ -1570,18 +1566,14 @@ template <int GRP, class T, int ND> struct Ops
 		int lt[4]; // log2 tile extents
 		int threads, minb;
 		char const *name;
-		int f2 = 0;        // packed FP32x2 products, pairing 1 or 2 (SU(3) float only)
-		bool full = false; // read all 18 reals of SU(3) FP32 links even where rows 0, 1 would do
+		int f2 = 0;        // packed FP32x2 products (SU(3) float only)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
-	// packed FP32x2 products; 14-17 and 21-22: thread per site
-	// (k_momentum_step_site) with FP32x2 products; 18-20: thread per site,
-	// plain products; 23-24: thread per site, FP32x2, whole links read (no
-	// row rebuilt: fewer products, more bytes through L1); 25-26: thread per
-	// site, FP32x2 with the second pairing (broadcast left factor); 27-32:
-	// thread per site, FP32x2, 128 threads x 4 blocks, other tile shapes
-	static constexpr int kForceVariants = 33;
+	// packed FP32x2 products; 14-17, 21-28: thread per site
+	// (k_momentum_step_site) with FP32x2 products, tiles and launch shapes;
+	// 18-20: thread per site, plain products (every group and precision)
+	static constexpr int kForceVariants = 29;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1609,10 +1601,6 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 2, 2, 3}, 256, 2, "site/tile2x4x4x8/256thr/2blk"},
 		    {2, {2, 2, 2, 3}, 512, 1, "site/tile4x4x4x8/512thr/1blk/f32x2", true},
 		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2", true},
-		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/full", true, true},
-		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2/full", true, true},
-		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2b", 2},
-		    {2, {1, 2, 3, 3}, 512, 1, "site/tile2x4x8x8/512thr/1blk/f32x2b", 2},
 		    {2, {0, 1, 3, 3}, 128, 4, "site/tile1x2x8x8/128thr/4blk/f32x2", 1},
 		    {2, {1, 2, 2, 2}, 128, 4, "site/tile2x4x4x4/128thr/4blk/f32x2", 1},
 		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/f32x2", 1},
@@ -1640,7 +1628,7 @@ template <int GRP, class T, int ND> struct Ops
 	static void launch_force(int v, Field &P, Field const &U, T coef, RedSlot kin, bool rows = false)
 	{
 		if constexpr (kRows<GRP, T>)
-			if (rows && !force_variant(v).full)
+			if (rows)
 				return launch_force_t<true>(v, P, U, coef, kin);
 		launch_force_t<false>(v, P, U, coef, kin);
 	}
@@ -1702,16 +1690,13 @@ template <int GRP, class T, int ND> struct Ops
 		{
 			if constexpr (kF2)
 			{
-				if (fv.f2 == 2)
-					return site_cfg<2, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
-				if (fv.f2 == 1)
+				if (fv.f2)
 					return site_cfg<1, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
 			}
 			site_cfg<0, ROWS, false>(fv, b, g, ts, u, p, coef, kin, c, nullptr, T(0), 0);
 		}
 	}
-	// the launch configurations of the thread-per-site kernel (pairing 2 only
-	// in the 128x4 and 512x1 configurations)
+	// the launch configurations of the thread-per-site kernel
 	template <int F2, bool ROWS, bool FUSE>
 	static void site_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u, T *p,
 	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
@@ -1719,18 +1704,15 @@ template <int GRP, class T, int ND> struct Ops
 		if (fv.threads == 512)
 			k_momentum_step_site<GRP, T, 4, 512, 1, F2, ROWS, FUSE>
 			    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-		else if (F2 == 2 || (fv.threads == 128 && fv.minb == 4))
+		else if (fv.threads == 128 && fv.minb == 4)
 			k_momentum_step_site<GRP, T, 4, 128, 4, F2, ROWS, FUSE>
 			    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-		else if constexpr (F2 != 2)
-		{
-			if (fv.threads == 128)
-				k_momentum_step_site<GRP, T, 4, 128, 3, F2, ROWS, FUSE>
-				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-			else
-				k_momentum_step_site<GRP, T, 4, 256, 2, F2, ROWS, FUSE>
-				    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-		}
+		else if (fv.threads == 128)
+			k_momentum_step_site<GRP, T, 4, 128, 3, F2, ROWS, FUSE>
+			    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+		else
+			k_momentum_step_site<GRP, T, 4, 256, 2, F2, ROWS, FUSE>
+			    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 	}
 	// tiles of variant fv over g and the grid size (at most minb blocks per SM)
 	static TileSpec tiles_for(Geom const &g, ForceVariant const &fv, Context const &c, unsigned &b)
@@ -1750,7 +1732,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 32; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 28; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
@@ -1762,10 +1744,7 @@ template <int GRP, class T, int ND> struct Ops
 	}
 	static void launch_md(int v, Field &P, Field const &Uin, Field &Uout, T coef, T tu, int reunit, RedSlot kin)
 	{
-		if (force_variant(v).full)
-			launch_md_t<false>(v, P, Uin, Uout, coef, tu, reunit, kin);
-		else
-			launch_md_t<kRows<GRP, T>>(v, P, Uin, Uout, coef, tu, reunit, kin);
+		launch_md_t<kRows<GRP, T>>(v, P, Uin, Uout, coef, tu, reunit, kin);
 	}
 	template <bool R>
 	static void launch_md_t(int v, Field &P, Field const &Uin, Field &Uout, T coef, T tu, int reunit, RedSlot kin)
@@ -1782,9 +1761,7 @@ template <int GRP, class T, int ND> struct Ops
 			T *uo = static_cast<T *>(Uout.d);
 			if constexpr (kF2)
 			{
-				if (fv.f2 == 2)
-					site_cfg<2, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
-				else if (fv.f2 == 1)
+				if (fv.f2)
 					site_cfg<1, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
 				else
 					site_cfg<0, R, true>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
