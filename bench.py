@@ -48,11 +48,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattice", type=int, default=32,
                     help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
-    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson", "heatbath"], default="hmc",
+    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson", "heatbath", "config1"], default="hmc",
                     help="hmc: the headline line; batch: 64 SU(2) replicas in one persistent launch against 64 "
                          "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
                          "(plain and learned multiplier); wilson: all r x t Wilson loops of a thermalised "
-                         "configuration; heatbath: heat-bath + overrelaxation sweeps")
+                         "configuration; heatbath: heat-bath + overrelaxation sweeps; config1: the FP64 8^4 "
+                         "cold-start chain against the CPU oracle, trajectory by trajectory")
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
     ap.add_argument("--fp64", action="store_true",
                     help="hmc workload: the plain all-FP64 chain (links, momenta, force in FP64) instead of the "
@@ -463,6 +464,47 @@ def run_batch(args):
     return 0
 
 
+def run_config1(args):
+    """SU(3) 8^4, beta = 5.7, FP64, cold start, 20 trajectories of 2lf
+    epsilon = 0.5 n = 10 (tau = 1), momenta from seed 1234: plaquette, dH
+    and accept per trajectory on the GPU chain and on the CPU oracle's chain
+    (same counter-based streams), with trajectories per second of both."""
+    import numpy as np
+    import torch
+
+    import mesh_gb300 as mg
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    dims, beta, seed, ntraj = [8, 8, 8, 8], 5.7, 1234, 20
+    d = mg.make_deltas("2lf", 0.5, 10)
+    ctx = mg.Context(0)
+    h = mg.Hmc(ctx, 3, mg.F64, mg.Grid(dims), seed=seed)
+    h.cold_start()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    recs = [h.update(beta, d) for _ in range(ntraj)]
+    t_gpu = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, ro = pyoracle.hmc_chain(3, 2, dims, pyoracle.unit_gauge(3, 2, dims), beta, pyoracle.make_deltas("2lf", 0.5, 10),
+                               seed, 0, ntraj)
+    t_cpu = time.perf_counter() - t0
+    rows = [{"traj": k, "plaq_gpu": r["plaquette"], "plaq_oracle": float(ro[k, 0]), "dH_gpu": r["dH"],
+             "dH_oracle": float(ro[k, 1]), "accept_gpu": r["accept"], "accept_oracle": float(ro[k, 2])}
+            for k, r in enumerate(recs)]
+    out = {"metric": "SU(3) 8^4 FP64 HMC trajectories/s (cold start, per-trajectory parity)", "value": ntraj / t_gpu,
+           "unit": "traj/s", "n_gpus": 1, "steps": ntraj, "higher_is_better": True, "dtype": "f64",
+           "data": "synthetic", "config": {"workload": "su3_hmc_8^4_beta5.7_2lf_eps0.5_n10_fp64_cold_seed1234"},
+           "cpu_oracle_traj_per_s": ntraj / t_cpu, "cpu_cores": pyoracle.set_threads(0),
+           "max_abs_diff": {"plaquette": max(abs(r["plaq_gpu"] - r["plaq_oracle"]) for r in rows),
+                            "dH": max(abs(r["dH_gpu"] - r["dH_oracle"]) for r in rows)},
+           "accept_agree": all(r["accept_gpu"] == r["accept_oracle"] for r in rows), "rows": rows}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_heatbath(args):
     """Heat-bath + overrelaxation updates of SU(3) L^4 at beta = 6.0 in FP32
     (one heat-bath and three overrelaxation sweeps per step, from a cold start
@@ -595,6 +637,8 @@ def main():
         return run_wilson(args)
     if args.workload == "heatbath":
         return run_heatbath(args)
+    if args.workload == "config1":
+        return run_config1(args)
     return run_ours(args)
 
 
