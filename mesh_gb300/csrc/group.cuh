@@ -121,7 +121,11 @@ template <class T> struct Group<U1, T>
 	}
 	MESH_HD static E reunit_fast(E a)
 	{
-		T f = T(1.5) - (a.v[0] * a.v[0] + a.v[1] * a.v[1]) * T(0.5);
+		T f;
+		if constexpr (sizeof(T) == 4) // |a|^2 - 1 accumulated from -1 (no rounding at 1.0)
+			f = T(1) - fmaf(a.v[0], a.v[0], fmaf(a.v[1], a.v[1], T(-1))) * T(0.5);
+		else
+			f = T(1.5) - (a.v[0] * a.v[0] + a.v[1] * a.v[1]) * T(0.5);
 		return {{a.v[0] * f, a.v[1] * f}};
 	}
 	MESH_HD static E reunit_exact(E a)
@@ -212,8 +216,15 @@ template <class T> struct Group<SU2, T>
 	}
 	MESH_HD static E reunit_fast(E a)
 	{
-		T n = a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2] + a.v[3] * a.v[3];
-		T f = T(1.5) - n * T(0.5);
+		T f;
+		if constexpr (sizeof(T) == 4) // |a|^2 - 1 accumulated from -1 (no rounding at 1.0)
+			f = T(1) - fmaf(a.v[0], a.v[0], fmaf(a.v[1], a.v[1], fmaf(a.v[2], a.v[2], fmaf(a.v[3], a.v[3], T(-1))))) *
+			               T(0.5);
+		else
+		{
+			T n = a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2] + a.v[3] * a.v[3];
+			f = T(1.5) - n * T(0.5);
+		}
 		return {{a.v[0] * f, a.v[1] * f, a.v[2] * f, a.v[3] * f}};
 	}
 	MESH_HD static E reunit_exact(E a)
@@ -602,12 +613,45 @@ template <class T> struct Group<SU3, T>
 	// r = 1.5 a - 0.5 a a^dagger a;  r (4/3 - det(r)/3)
 	MESH_HD static E reunit_fast(E const &a)
 	{
-		E aa = mul_nd(a, a);
-		E aaa = mul(aa, a);
 		E r;
+		if constexpr (sizeof(T) == 4)
+		{
+			// FP32: the same r = a - (a a^dagger - 1) a / 2 with the deviation
+			// a a^dagger - 1 accumulated from -1, so that no sum is rounded at
+			// 1.0, where the float grid is twice as fine below as above and
+			// rounding pulls the norms of nearly unitary rows down on average
+			// (1.5 a - 0.5 (a a^dagger) a in FP32 leaves |det| 2e-8 above 1)
+			E dev;
 #pragma unroll
-		for (int k = 0; k < 18; ++k)
-			r.v[k] = a.v[k] * T(1.5) - aaa.v[k] * T(0.5);
+			for (int i = 0; i < 3; ++i)
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+				{
+					T re = i == j ? T(-1) : T(0), im = T(0);
+#pragma unroll
+					for (int k = 0; k < 3; ++k)
+					{
+						T ar = a.v[6 * i + 2 * k], ai = a.v[6 * i + 2 * k + 1];
+						T br = a.v[6 * j + 2 * k], bi = a.v[6 * j + 2 * k + 1];
+						re = fmaf(ar, br, fmaf(ai, bi, re));
+						im = fmaf(ai, br, fmaf(-ar, bi, im));
+					}
+					dev.v[6 * i + 2 * j] = re;
+					dev.v[6 * i + 2 * j + 1] = im;
+				}
+			E da = mul(dev, a);
+#pragma unroll
+			for (int k = 0; k < 18; ++k)
+				r.v[k] = a.v[k] - da.v[k] * T(0.5);
+		}
+		else
+		{
+			E aa = mul_nd(a, a);
+			E aaa = mul(aa, a);
+#pragma unroll
+			for (int k = 0; k < 18; ++k)
+				r.v[k] = a.v[k] * T(1.5) - aaa.v[k] * T(0.5);
+		}
 		cx<T> d = det(r);
 		cx<T> f = {T(4.0 / 3.0) - d.re * T(1.0 / 3.0), -d.im * T(1.0 / 3.0)};
 		E o;
