@@ -121,11 +121,15 @@ template <class T> struct Group<U1, T>
 	}
 	MESH_HD static E reunit_fast(E a)
 	{
-		T f;
-		if constexpr (sizeof(T) == 4) // |a|^2 - 1 accumulated from -1 (no rounding at 1.0)
-			f = T(1) - fmaf(a.v[0], a.v[0], fmaf(a.v[1], a.v[1], T(-1))) * T(0.5);
-		else
-			f = T(1.5) - (a.v[0] * a.v[0] + a.v[1] * a.v[1]) * T(0.5);
+		if constexpr (sizeof(T) == 4)
+		{
+			// a - a (|a|^2 - 1) / 2 with |a|^2 - 1 accumulated from -1: no
+			// quantity near 1.0 is rounded (the float grid is twice as fine
+			// below 1 as above, which biases such roundings)
+			T g = fmaf(a.v[0], a.v[0], fmaf(a.v[1], a.v[1], T(-1))) * T(-0.5);
+			return {{fmaf(a.v[0], g, a.v[0]), fmaf(a.v[1], g, a.v[1])}};
+		}
+		T f = T(1.5) - (a.v[0] * a.v[0] + a.v[1] * a.v[1]) * T(0.5);
 		return {{a.v[0] * f, a.v[1] * f}};
 	}
 	MESH_HD static E reunit_exact(E a)
@@ -216,15 +220,16 @@ template <class T> struct Group<SU2, T>
 	}
 	MESH_HD static E reunit_fast(E a)
 	{
-		T f;
-		if constexpr (sizeof(T) == 4) // |a|^2 - 1 accumulated from -1 (no rounding at 1.0)
-			f = T(1) - fmaf(a.v[0], a.v[0], fmaf(a.v[1], a.v[1], fmaf(a.v[2], a.v[2], fmaf(a.v[3], a.v[3], T(-1))))) *
-			               T(0.5);
-		else
+		if constexpr (sizeof(T) == 4)
 		{
-			T n = a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2] + a.v[3] * a.v[3];
-			f = T(1.5) - n * T(0.5);
+			// a - a (|a|^2 - 1) / 2, no quantity near 1.0 rounded (see U(1))
+			T g = fmaf(a.v[0], a.v[0], fmaf(a.v[1], a.v[1], fmaf(a.v[2], a.v[2], fmaf(a.v[3], a.v[3], T(-1))))) *
+			      T(-0.5);
+			return {{fmaf(a.v[0], g, a.v[0]), fmaf(a.v[1], g, a.v[1]), fmaf(a.v[2], g, a.v[2]),
+			         fmaf(a.v[3], g, a.v[3])}};
 		}
+		T n = a.v[0] * a.v[0] + a.v[1] * a.v[1] + a.v[2] * a.v[2] + a.v[3] * a.v[3];
+		T f = T(1.5) - n * T(0.5);
 		return {{a.v[0] * f, a.v[1] * f, a.v[2] * f, a.v[3] * f}};
 	}
 	MESH_HD static E reunit_exact(E a)
@@ -652,14 +657,33 @@ template <class T> struct Group<SU3, T>
 			for (int k = 0; k < 18; ++k)
 				r.v[k] = a.v[k] * T(1.5) - aaa.v[k] * T(0.5);
 		}
-		cx<T> d = det(r);
-		cx<T> f = {T(4.0 / 3.0) - d.re * T(1.0 / 3.0), -d.im * T(1.0 / 3.0)};
 		E o;
+		if constexpr (sizeof(T) == 4)
+		{
+			// r (4/3 - det r / 3) = r + r g with g = -(det r - 1) / 3, det r - 1
+			// accumulated from -1 (no quantity near 1.0 rounded)
+			cx<T> A = csub(cmul(r.at(1, 1), r.at(2, 2)), cmul(r.at(1, 2), r.at(2, 1)));
+			cx<T> B = csub(cmul(r.at(1, 0), r.at(2, 2)), cmul(r.at(1, 2), r.at(2, 0)));
+			cx<T> Cc = csub(cmul(r.at(1, 0), r.at(2, 1)), cmul(r.at(1, 1), r.at(2, 0)));
+			cx<T> t0 = cmul(r.at(0, 0), A), t1 = cmul(r.at(0, 1), B), t2 = cmul(r.at(0, 2), Cc);
+			cx<T> dm1 = {((T(-1) + t0.re) - t1.re) + t2.re, (t0.im - t1.im) + t2.im};
+			cx<T> g = {dm1.re * T(-1.0 / 3.0), dm1.im * T(-1.0 / 3.0)};
 #pragma unroll
-		for (int i = 0; i < 3; ++i)
+			for (int i = 0; i < 3; ++i)
 #pragma unroll
-			for (int j = 0; j < 3; ++j)
-				o.set(i, j, cmul(r.at(i, j), f));
+				for (int j = 0; j < 3; ++j)
+					o.set(i, j, cadd(r.at(i, j), cmul(r.at(i, j), g)));
+		}
+		else
+		{
+			cx<T> d = det(r);
+			cx<T> f = {T(4.0 / 3.0) - d.re * T(1.0 / 3.0), -d.im * T(1.0 / 3.0)};
+#pragma unroll
+			for (int i = 0; i < 3; ++i)
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+					o.set(i, j, cmul(r.at(i, j), f));
+		}
 		return o;
 	}
 	// row 2 of a special unitary matrix from rows 0 and 1: conj(row0 x row1)
