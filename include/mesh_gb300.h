@@ -360,9 +360,15 @@ int mesh_landau_fa_theta(mesh_landau_fa h, mesh_field g, double *theta);
 /* one step in place; theta of g before the step */
 int mesh_landau_fa_step(mesh_landau_fa h, mesh_field g, double *theta_before);
 /* steps until theta < tol; a step that does not lower theta is undone and
- * or_sweeps overrelaxation sweeps (omega) run instead (the fallback) */
+ * or_sweeps overrelaxation sweeps (omega) run instead (the fallback). With
+ * mesh_landau_fa_set_accept(h, 1) the test is on the gauge functional
+ * instead: a step is undone when it lowered sum Re tr g U g^+ by more than
+ * its FP64 summation error (theta, the norm of the gradient, may rise for a
+ * step while the functional rises) */
 int mesh_landau_fa_run(mesh_landau_fa h, mesh_field g, double tol, int max_iter, double omega, int or_sweeps,
                        int *iters, int *fallbacks, double *theta);
+/* acceptance test of mesh_landau_fa_run: 0 = theta (default), 1 = the gauge functional */
+int mesh_landau_fa_set_accept(mesh_landau_fa h, int on_functional);
 /* trial step that leaves g unchanged (the current multiplier, or the plain
  * one with alpha when alpha > 0): theta before and after */
 int mesh_landau_fa_trial(mesh_landau_fa h, mesh_field g, double alpha, double *theta_before, double *theta_after);

@@ -139,6 +139,7 @@ SIGNATURES = {
     "mesh_landau_fa_theta": (_I, [_P, _P, _DP]),
     "mesh_landau_fa_step": (_I, [_P, _P, _DP]),
     "mesh_landau_fa_run": (_I, [_P, _P, _D, _I, _D, _I, _IP, _IP, _DP]),
+    "mesh_landau_fa_set_accept": (_I, [_P, _I]),
     "mesh_landau_fa_probe": (_I, [_P, _P, _D, _I, _DP, _DP, _DP, _DP, _DP]),
     "mesh_landau_fa_trial": (_I, [_P, _P, _D, _DP, _DP]),
     "mesh_lattice_fft": (_I, [_P, _I, _I32P, _I, C.POINTER(C.c_float), _I]),
@@ -757,6 +758,10 @@ class LandauFA:
         t = C.c_double()
         _chk(load().mesh_landau_fa_step(self.h, g.h, C.byref(t)))
         return t.value
+
+    def set_accept(self, functional: bool):
+        """acceptance test of run(): on theta (default) or on the gauge functional"""
+        _chk(load().mesh_landau_fa_set_accept(self.h, 1 if functional else 0))
 
     def run(self, g: Field, tol=1e-12, max_iter=100000, omega=1.7, or_sweeps=10, raise_on_noconv=False):
         it, fb, th = C.c_int(), C.c_int(), C.c_double()

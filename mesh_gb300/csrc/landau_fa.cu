@@ -13,19 +13,19 @@ namespace {
 
 struct FaTable
 {
-	void (*links)(Field const &U, Field const &g, double *A);
+	void (*links)(Field const &U, Field const &g, double *A, RedSlot func);
 	void (*div)(Field const &U, double const *A, float2 *buf, RedSlot theta);
 	void (*update)(Field const &U, float2 const *buf, Field const &gin, double *gout);
 };
 
 template <int GRP, int ND> struct FaOps
 {
-	static void links(Field const &U, Field const &g, double *A)
+	static void links(Field const &U, Field const &g, double *A, RedSlot func)
 	{
 		auto &c = *U.ctx;
 		int64_t n = int64_t(ND) * U.geom.V;
 		k_fa_links<GRP, double, ND><<<grid_for(c, n, 256), 256, 0, c.stream>>>(
-		    U.geom, static_cast<double const *>(U.d), static_cast<double const *>(g.d), A);
+		    U.geom, static_cast<double const *>(U.d), static_cast<double const *>(g.d), A, func);
 		MESH_LAUNCH_CHECK();
 	}
 	static void div(Field const &U, double const *A, float2 *buf, RedSlot theta)
@@ -88,9 +88,14 @@ struct mesh_landau_fa_s
 	double *A = nullptr; // nd x NA x V
 	float2 *buf = nullptr, *buf_old = nullptr;
 	double *g_trial = nullptr;
-	double *red = nullptr; // partials + result + counter for theta
+	// reduction scratch, two slots (0: theta, 1: the gauge functional):
+	// partials, results, counters
+	double *red = nullptr;
 	double *res = nullptr;
 	unsigned *cnt = nullptr;
+	// accept a descent step when the gauge functional did not drop (instead
+	// of when theta dropped)
+	bool accept_functional = false;
 	float *table = nullptr; // learned multiplier table (device)
 	MomTables mt{};
 	Multiplier mult{};
@@ -105,7 +110,7 @@ struct mesh_landau_fa_s
 	double *shell = nullptr;
 	int shell_bins = 0;
 
-	RedSlot slot() { return {red, res, cnt}; }
+	RedSlot slot(int k = 0) { return {red + size_t(k) * kMaxRedBlocks, res + k, cnt + k}; }
 
 	~mesh_landau_fa_s()
 	{
@@ -133,20 +138,18 @@ struct mesh_landau_fa_s
 		mlp_forward_device(*ctx, mlp_n, mlp_x, mlp_params, mlp_width, mlp_bf16, table);
 	}
 
-	double read_theta()
+	// theta of g; leaves Delta (FP32 complex) in buf when want_buf; with
+	// `func`, also the sum of Re tr g(x) U_mu(x) g(x+mu)^+ over all links
+	double theta(Field const &g, bool want_buf, double *func = nullptr)
 	{
-		double v = 0;
-		MESH_CUDA(cudaMemcpyAsync(&v, res, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+		tab->links(*U, g, A, func ? slot(1) : RedSlot{nullptr, nullptr, nullptr});
+		tab->div(*U, A, want_buf ? buf : nullptr, slot(0));
+		double v[2] = {0, 0};
+		MESH_CUDA(cudaMemcpyAsync(v, res, sizeof(double) * (func ? 2 : 1), cudaMemcpyDeviceToHost, ctx->stream));
 		MESH_CUDA(cudaStreamSynchronize(ctx->stream));
-		return v / (double(U->nd) * double(U->geom.V));
-	}
-
-	// theta of g; leaves Delta (FP32 complex) in buf when want_buf
-	double theta(Field const &g, bool want_buf)
-	{
-		tab->links(*U, g, A);
-		tab->div(*U, A, want_buf ? buf : nullptr, slot());
-		return read_theta();
+		if (func)
+			*func = v[1];
+		return v[0] / (double(U->nd) * double(U->geom.V));
 	}
 
 	// step on buf (Delta of g already there): gout = reunit(exp(-F^-1[m F Delta]/V) gin)
@@ -190,10 +193,10 @@ int mesh_landau_fa_create(mesh_field Uh, mesh_landau_fa_s **out)
 		MESH_CUDA(cudaMalloc(&h->buf, sizeof(float2) * size_t(h->nf) * V));
 		MESH_CUDA(cudaMalloc(&h->buf_old, sizeof(float2) * size_t(h->nf) * V));
 		MESH_CUDA(cudaMalloc(&h->g_trial, sizeof(double) * size_t(group_nr(U.group)) * V));
-		MESH_CUDA(cudaMalloc(&h->red, sizeof(double) * kMaxRedBlocks));
-		MESH_CUDA(cudaMalloc(&h->res, sizeof(double)));
-		MESH_CUDA(cudaMalloc(&h->cnt, sizeof(unsigned)));
-		MESH_CUDA(cudaMemset(h->cnt, 0, sizeof(unsigned)));
+		MESH_CUDA(cudaMalloc(&h->red, sizeof(double) * 2 * kMaxRedBlocks));
+		MESH_CUDA(cudaMalloc(&h->res, sizeof(double) * 2));
+		MESH_CUDA(cudaMalloc(&h->cnt, sizeof(unsigned) * 2));
+		MESH_CUDA(cudaMemset(h->cnt, 0, sizeof(unsigned) * 2));
 		MomTables &mt = h->mt;
 		mt.nd = U.nd;
 		int64_t st = 1;
@@ -365,9 +368,19 @@ int mesh_landau_fa_step(mesh_landau_fa_s *h, mesh_field gh, double *theta_before
 	});
 }
 
-// Steps until theta < tol. Every step is checked on the next theta: if it
-// did not lower theta, it is undone and `or_sweeps` overrelaxation sweeps
-// (omega) run instead. iters counts steps taken, fallbacks the OR blocks.
+int mesh_landau_fa_set_accept(mesh_landau_fa_s *h, int on_functional)
+{
+	return fa_api([&] {
+		require(h != nullptr && (on_functional == 0 || on_functional == 1), "invalid argument");
+		h->accept_functional = on_functional == 1;
+	});
+}
+
+// Steps until theta < tol. Every step is checked: by default a step that did
+// not lower theta, with mesh_landau_fa_set_accept(h, 1) one that lowered the
+// gauge functional (by more than its FP64 summation error), is undone and
+// `or_sweeps` overrelaxation sweeps (omega) run instead. iters counts steps
+// taken, fallbacks the OR blocks.
 int mesh_landau_fa_run(mesh_landau_fa_s *h, mesh_field gh, double tol, int max_iter, double omega, int or_sweeps,
                        int *iters, int *fallbacks, double *theta_out)
 {
@@ -382,7 +395,11 @@ int mesh_landau_fa_run(mesh_landau_fa_s *h, mesh_field gh, double tol, int max_i
 		Context &c = *h->ctx;
 		Field trial = g;
 		trial.d = h->g_trial;
-		double th = h->theta(g, true);
+		bool by_f = h->accept_functional;
+		double f = 0, f_new = 0;
+		double th = h->theta(g, true, by_f ? &f : nullptr);
+		// FP64 summation error of the functional sum (Nd V terms of size <= Nc)
+		double f_tol = 1e-15 * double(group_nc(h->U->group)) * double(h->U->nd) * double(h->U->geom.V);
 		int it = 0, fb = 0;
 		while (!(th < tol) && it < max_iter)
 		{
@@ -390,11 +407,12 @@ int mesh_landau_fa_run(mesh_landau_fa_s *h, mesh_field gh, double tol, int max_i
 				throw Error(MESH_ERR_NUMERIC, "non-finite gauge condition theta");
 			h->step_from_buf(g, h->g_trial, h->mult, th);
 			++it;
-			double th_new = h->theta(trial, true);
-			if (th_new < th)
+			double th_new = h->theta(trial, true, by_f ? &f_new : nullptr);
+			if (by_f ? (std::isfinite(th_new) && f_new > f - f_tol) : th_new < th)
 			{
 				MESH_CUDA(cudaMemcpyAsync(g.d, h->g_trial, g.bytes, cudaMemcpyDeviceToDevice, c.stream));
 				th = th_new;
+				f = f_new;
 			}
 			else
 			{
@@ -406,7 +424,7 @@ int mesh_landau_fa_run(mesh_landau_fa_s *h, mesh_field gh, double tol, int max_i
 					ops.landau_or_half(*h->U, g, omega, 1);
 				}
 				ops.reunit_exact(g);
-				th = h->theta(g, true);
+				th = h->theta(g, true, by_f ? &f : nullptr);
 			}
 		}
 		if (iters)
@@ -476,7 +494,7 @@ int mesh_landau_fa_probe(mesh_landau_fa_s *h, mesh_field gh, double probe_alpha,
 		h->tab->update(*h->U, h->buf, g, h->g_trial);
 		Field trial = g;
 		trial.d = h->g_trial;
-		h->tab->links(*h->U, trial, h->A);
+		h->tab->links(*h->U, trial, h->A, RedSlot{nullptr, nullptr, nullptr});
 		h->tab->div(*h->U, h->A, h->buf, h->slot());
 		fft::fft_nd<-1>(h->buf, h->U->nd, h->U->dims, h->nf, c.num_sms, c.stream);
 		if (h->shell_bins != nbins)

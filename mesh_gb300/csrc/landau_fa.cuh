@@ -5,7 +5,9 @@
 // No counterpart in the reference (its solver is the CG of landau.h:100-136).
 //
 // One step on the gauge transform g (FP64), links U fixed:
-//   A_mu(x)   = proj(g(x) U_mu(x) g(x+mu)^+)                 k_fa_links (FP64)
+//   A_mu(x)   = proj(g(x) U_mu(x) g(x+mu)^+)                 k_fa_links (FP64;
+//               optionally the FP64 sum of Re tr g(x) U_mu(x) g(x+mu)^+,
+//               the gauge functional up to its normalisation)
 //   Delta(x)  = sum_mu A_mu(x) - A_mu(x-mu)                   k_fa_div   (FP64;
 //               theta_ref = sum |Delta|^2/(Nd V) in FP64; Delta packed
 //               pairwise into FP32 complex fields, lexicographic order)
@@ -74,8 +76,9 @@ __device__ __forceinline__ float mult_of(Multiplier const &m, MomTables const &m
 // A_mu(x) for every link, packed algebra, SoA per direction
 template <int GRP, class T, int ND>
 __global__ void __launch_bounds__(256) k_fa_links(Geom g, T const *__restrict__ U, T const *__restrict__ G,
-                                                   T *__restrict__ A)
+                                                   T *__restrict__ A, RedSlot func)
 {
+	double acc = 0.0;
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	LinkLoad<GRP, T, ND> ld{U, g.V};
@@ -89,9 +92,14 @@ __global__ void __launch_bounds__(256) k_fa_links(Geom g, T const *__restrict__ 
 		Soa<T, Gp::NR>::load(G, g.V, s, gx.v);
 		Soa<T, Gp::NR>::load(G, g.V, eo_shift1<ND>(g, st, mu, +1), gf.v);
 		T a[Gp::NA];
-		Gp::proj(Gp::mul_nd(Gp::mul(gx, ld(mu, s)), gf), a);
+		E w = Gp::mul_nd(Gp::mul(gx, ld(mu, s)), gf);
+		if (func.result)
+			acc += double(Gp::retr(w));
+		Gp::proj(w, a);
 		comp<T, Gp::NA>(A, g.V, mu).store(s, a);
 	}
+	if (func.result) // uniform over the grid (a kernel argument)
+		grid_sum<256>(acc, func);
 }
 
 // Delta(x), theta sum, and the FP32 complex FFT input (lexicographic order)

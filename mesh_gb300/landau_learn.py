@@ -203,9 +203,10 @@ def train(ctx, data, epochs=200, batch=1024, lr=2e-3, seed=0):
     return params, losses
 
 
-def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omega=1.7):
+def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omega=1.7, accept="theta"):
     """Fix U to Landau gauge from g = 1 with `method` in {"or", "plain", "learned"};
-    returns dict(seconds, iterations, fallbacks, theta, functional)."""
+    Fourier-accelerated steps are accepted on `accept` ("theta" or
+    "functional"); returns dict(seconds, iterations, fallbacks, theta, functional)."""
     import torch
 
     g = Lattice(U.ctx, 3, F64, U.grid).set_unit()
@@ -219,6 +220,7 @@ def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omeg
         fb = 0
     else:
         fa = LandauFA(U)
+        fa.set_accept(accept == "functional")
         if method == "plain":
             fa.set_plain(PLAIN_ALPHA)
         else:

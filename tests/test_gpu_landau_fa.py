@@ -107,6 +107,33 @@ def test_fa_fallback_to_overrelaxation(ctx, oracle):
     assert th < 1e-12 and fb > 0
 
 
+def test_fa_functional_acceptance(ctx, oracle):
+    """steps accepted on the gauge functional instead of theta: the stable
+    step size converges to the same functional as the theta-accepted run (a
+    Gribov copy may differ at 1e-4), and an unstable one is still caught
+    (fallbacks) and converges"""
+    dims = [8, 8, 8, 8]
+    U64 = fixed_problem(oracle, 3, dims)
+    U = mg.GaugeField(ctx, 3, mg.F64, mg.Grid(dims)).import_(U64)
+    L = mg.Landau(U)
+    func = {}
+    for accept in (False, True):
+        for alpha in (0.08, 0.3):
+            fa = mg.LandauFA(U)
+            fa.set_plain(alpha)
+            fa.set_accept(accept)
+            gt = mg.Lattice(ctx, 3, mg.F64, mg.Grid(dims)).set_unit()
+            it, fb, th = fa.run(gt, tol=1e-12, max_iter=3000, omega=1.7, or_sweeps=10)
+            fa.close()
+            assert th < 1e-12
+            if alpha == 0.3:
+                assert fb > 0
+            L.g.import_(gt.export())
+            func[accept, alpha] = L()
+    assert func[True, 0.08] == pytest.approx(func[False, 0.08], rel=1e-4)
+    assert 0.5 < func[True, 0.3] < 1.0
+
+
 def test_fa_probe_response_is_physical(ctx, oracle):
     dims = [8, 8, 8, 8]
     U64 = fixed_problem(oracle, 3, dims)
