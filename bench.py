@@ -48,11 +48,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--lattice", type=int, default=32,
                     help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
-    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson", "heatbath", "config1"], default="hmc",
+    ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson", "heatbath", "fp64-8x4"], default="hmc",
                     help="hmc: the headline line; batch: 64 SU(2) replicas in one persistent launch against 64 "
                          "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
                          "(plain and learned multiplier); wilson: all r x t Wilson loops of a thermalised "
-                         "configuration; heatbath: heat-bath + overrelaxation sweeps; config1: the FP64 8^4 "
+                         "configuration; heatbath: heat-bath + overrelaxation sweeps; fp64-8x4: the FP64 8^4 "
                          "cold-start chain against the CPU oracle, trajectory by trajectory")
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
     ap.add_argument("--fa-accept", choices=["theta", "functional"], default="theta",
@@ -467,7 +467,7 @@ def run_batch(args):
     return 0
 
 
-def run_config1(args):
+def run_fp64_8x4(args):
     """SU(3) 8^4, beta = 5.7, FP64, cold start, 20 trajectories of 2lf
     epsilon = 0.5 n = 10 (tau = 1), momenta from seed 1234: plaquette, dH
     and accept per trajectory on the GPU chain and on the CPU oracle's chain
@@ -649,8 +649,8 @@ def main():
         return run_wilson(args)
     if args.workload == "heatbath":
         return run_heatbath(args)
-    if args.workload == "config1":
-        return run_config1(args)
+    if args.workload == "fp64-8x4":
+        return run_fp64_8x4(args)
     return run_ours(args)
 
 

@@ -1,5 +1,5 @@
 """The converted HMC driver (mesh_gb300/apps/hmc.cpp on include/mesh/mesh.hpp)
-runs the reference's configs[0] flow (SU(3) 8^4 beta 5.7, cold start, 2lf
+runs the reference app's own small chain (SU(3) 8^4 beta 5.7, cold start, 2lf
 eps 0.5 n 10, seed 1234, FP64) and matches the FP64 oracle chain; a run cut
 in two by --checkpoint / --resume prints the same trajectories."""
 import os

@@ -256,7 +256,7 @@ def test_hmc_update_fp64_matches_oracle_on_supplied_inputs(ctx, oracle, g):
         assert rel(h.U.export(), U64) < TOL64
 
 
-def test_config1_chain_matches_oracle(ctx, oracle):
+def test_fp64_8x4_cold_chain_matches_oracle(ctx, oracle):
     """SU(3) 8^4, beta=5.7, cold start, 20 trajectories of 2lf n=10 (tau=1),
     momenta from seed 1234: plaquette, dH and accept per trajectory. Momenta
     and uniforms come from each side's own counter-based streams (same
