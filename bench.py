@@ -183,6 +183,24 @@ def cpu_baseline_md(U_host, P_host, dims, n, beta, delta, threads=0):
 
 
 # ---------------------------------------------------------------------------
+def replica_seed(rank):
+    """each rank's chain is an independent replica: its own seed"""
+    return WORKLOAD["seed"] + rank
+
+
+def job_time_and_rate(ms, steps, world, dist=None, device="cpu"):
+    """(max over ranks of the timed region in ms, whole-job trajectories/s):
+    every rank ran `steps` trajectories of its own replica, so the job did
+    world x steps in the slowest rank's time"""
+    if dist is not None:
+        import torch
+
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * steps / (ms / 1000.0)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -248,7 +266,7 @@ def run_ours(args):
     # link update after it, plaquette, metropolis, accept copy
     launches_per_traj = 1 + 1 + n_p + 1 + 2
     pb = WORKLOAD["prec_bytes"]
-    h = mg.Hmc(ctx, WORKLOAD["group"], mg.F64 if pb == 8 else mg.F32, grid, seed=WORKLOAD["seed"] + rank)
+    h = mg.Hmc(ctx, WORKLOAD["group"], mg.F64 if pb == 8 else mg.F32, grid, seed=replica_seed(rank))
     h.randomize_gauge_field()
     h.run(beta, d, args.therm, use_graph=True)
     h.run(beta, d, args.warmup, use_graph=True)
@@ -269,12 +287,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms / 1000.0)
+    ms, value = job_time_and_rate(e0.elapsed_time(e1), args.steps, world, dist, device="cuda")
     hist = h.history(h.count - args.steps - args.warmup - args.therm)
     acc = float(np.mean(hist["accept_history"][-args.steps:]))
     plaq = float(np.mean(hist["plaq_history"][args.therm:]))
