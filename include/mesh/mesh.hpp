@@ -499,6 +499,69 @@ template <class G> struct Landau
 	}
 };
 
+// ---- Fourier-accelerated Landau gauge fixing (no reference counterpart) ------------
+// Steepest descent with a spectral multiplier (plain alpha p2max/p^2, or the learned
+// MLP) on FP64 links; a step that fails the acceptance test (theta by default, or the
+// gauge functional) is undone and overrelaxation sweeps run instead. g is the gauge
+// transform, e.g. Landau<G>::g.
+template <class G> class LandauFA
+{
+  public:
+	static_assert(GaugeTraits<G>::precision == MESH_F64, "Fourier-accelerated gauge fixing runs on FP64 links");
+	struct Result
+	{
+		int iterations = 0, fallbacks = 0;
+		double theta = 0;
+	};
+
+	explicit LandauFA(GaugeField<G> const &U) { check(mesh_landau_fa_create(U.get(), &h_)); }
+	~LandauFA() { mesh_landau_fa_destroy(h_); }
+	LandauFA(LandauFA const &) = delete;
+	LandauFA &operator=(LandauFA const &) = delete;
+
+	void set_plain(double alpha = 0.08) { check(mesh_landau_fa_set_plain(h_, alpha)); }
+	// network parameters in the library's layout: width^2 + 6 width + 1 floats
+	void set_mlp(std::vector<float> const &params, int width, double beta, bool bf16 = true)
+	{
+		if (params.size() != size_t(width) * width + 6 * size_t(width) + 1)
+			throw std::runtime_error("MLP parameter count does not match the width");
+		check(mesh_landau_fa_set_mlp(h_, params.data(), width, beta, bf16 ? 1 : 0));
+	}
+	void accept_on_functional(bool on) { check(mesh_landau_fa_set_accept(h_, on ? 1 : 0)); }
+	double theta(Lattice<G> const &g) const
+	{
+		double t = 0;
+		check(mesh_landau_fa_theta(h_, g.get(), &t));
+		return t;
+	}
+	// steps until theta < tol; throws if max_iter steps do not reach it
+	Result run(Lattice<G> &g, double tol = 1e-12, int max_iter = 20000, double omega = 1.7, int or_sweeps = 10)
+	{
+		Result r;
+		check(mesh_landau_fa_run(h_, g.get(), tol, max_iter, omega, or_sweeps, &r.iterations, &r.fallbacks,
+		                         &r.theta));
+		return r;
+	}
+
+  private:
+	mesh_landau_fa h_ = nullptr;
+};
+
+// the committed network (mesh_gb300/landau_mlp_su3.f32): raw little-endian FP32 parameters
+inline std::vector<float> readMlpParams(std::string const &path)
+{
+	std::FILE *f = std::fopen(path.c_str(), "rb");
+	if (!f)
+		throw std::runtime_error("cannot open " + path);
+	std::vector<float> p;
+	float buf[1024];
+	size_t n;
+	while ((n = std::fread(buf, sizeof(float), 1024, f)) > 0)
+		p.insert(p.end(), buf, buf + n);
+	std::fclose(f);
+	return p;
+}
+
 // ---- runtime dispatch (utils.h:156-186) ------------------------------------------
 template <typename F> void dispatchByGroup(F f, std::string const &group, int precision)
 {

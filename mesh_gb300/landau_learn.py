@@ -27,7 +27,8 @@ Method (no counterpart in the reference; written for this library):
   lower theta (mesh_landau_fa_run).
 
 `python -m mesh_gb300.landau_learn train` regenerates the committed weights
-(landau_mlp_su3.npz) on a GPU; `... compare` prints the comparison.
+(landau_mlp_su3.npz, and the same parameters as raw FP32 in landau_mlp_su3.f32
+for C and C++ callers) on a GPU; `... compare` prints the comparison.
 """
 from __future__ import annotations
 
@@ -291,6 +292,8 @@ def main():
         np.savez(args.out, params=params, gamma=1.0, width=WIDTH, samples=len(data),
                  final_loss=float(losses[-1]), first_loss=float(losses[0]), configs=ncfg, lattice=args.L,
                  betas=betas)
+        # the same parameters as raw little-endian FP32 for C and C++ callers
+        np.asarray(params, dtype="<f4").tofile(os.path.splitext(args.out)[0] + ".f32")
         print(json.dumps({"samples": int(len(data)), "final_loss": float(losses[-1]),
                           "first_loss": float(losses[0]), "target_variance": float(np.var(data[:, 3])),
                           "t_generate_and_collect_s": t_collect, "configs": ncfg}))

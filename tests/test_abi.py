@@ -106,6 +106,27 @@ def test_cpp_dropin_app_compiles(libpath, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_cpp_landau_fa_instantiate(libpath, tmp_path):
+    """the C++ wrapper of the Fourier-accelerated solver compiles (FP64
+    groups only) and the raw FP32 copy of the committed network matches the
+    .npz the Python side loads"""
+    import numpy as np
+
+    src = tmp_path / "fa.cpp"
+    src.write_text('#include "mesh/mesh.hpp"\n'
+                   "template class mesh::LandauFA<mesh::SU3<double>>;\n"
+                   "template class mesh::LandauFA<mesh::U1<double>>;\n"
+                   "std::vector<float> f() { return mesh::readMlpParams(\"x.f32\"); }\n")
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Werror", "-c", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", str(tmp_path / "fa.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    z = np.load(os.path.join(ROOT, "mesh_gb300", "landau_mlp_su3.npz"))
+    raw = np.fromfile(os.path.join(ROOT, "mesh_gb300", "landau_mlp_su3.f32"), dtype="<f4")
+    w = int(z["width"])
+    assert raw.size == w * w + 6 * w + 1
+    assert np.array_equal(raw, z["params"].astype(np.float32))
+
+
 def test_cpp_wilson_loops_instantiate(libpath, tmp_path):
     """the drop-in wilson(), thermalize() and overrelax() (legacy
     src/old/mesh/wilson.cpp:40-75, src/old/wilson.cpp, gauge_action.h)

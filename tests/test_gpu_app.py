@@ -46,3 +46,52 @@ def test_app_matches_oracle_and_resumes(oracle, tmp_path):
     first = run(exe, *common, "--start", "cold", "--count", "3", "--checkpoint", ck)
     second = run(exe, *common, "--resume", ck, "--count", "3")
     np.testing.assert_array_equal(np.vstack([first, second]), full)
+
+
+LANDAU_FA_CPP = r"""
+#include "mesh/mesh.hpp"
+#include <cstdio>
+// Fourier-accelerated Landau gauge fixing through the C++ wrapper, with the
+// committed network, against the reference-style overrelaxation
+int main(int argc, char **argv)
+{
+	using G = mesh::SU3<double>;
+	if (argc < 2)
+		return 2;
+	mesh::Grid grid({8, 8, 8, 8});
+	mesh::GaugeField<G> U(grid);
+	U.set_unit();
+	for (uint64_t s = 0; s < 20; ++s)
+		mesh::thermalize(U, 6.0, 11, s);
+	mesh::Landau<G> L(U);
+	mesh::LandauFA<G> fa(U);
+	fa.set_mlp(mesh::readMlpParams(argv[1]), 64, 6.0);
+	auto r = fa.run(L.g);
+	std::printf("fa %d %d %.6e %.15f\n", r.iterations, r.fallbacks, r.theta, L());
+	mesh::Landau<G> L2(U);
+	int sweeps = L2.overrelax(1.7, 1e-12, 20000);
+	std::printf("or %d %.6e %.15f\n", sweeps, L2.condition(), L2());
+	return 0;
+}
+"""
+
+
+def test_cpp_landau_fa_learned(tmp_path):
+    import mesh_gb300.build as b
+
+    lib = b.build()
+    src = tmp_path / "fa.cpp"
+    src.write_text(LANDAU_FA_CPP)
+    exe = tmp_path / "fa"
+    subprocess.run(["g++", "-std=c++20", "-O2", "-I", os.path.join(ROOT, "include"), str(src), "-L",
+                    os.path.dirname(lib), "-lmesh_gb300", "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), os.path.join(ROOT, "mesh_gb300", "landau_mlp_su3.f32")], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    fa = re.search(r"fa (\d+) (\d+) (\S+) (\S+)", r.stdout)
+    orr = re.search(r"or (\d+) (\S+) (\S+)", r.stdout)
+    assert float(fa.group(3)) < 1e-12
+    f_fa, f_or = float(fa.group(4)), float(orr.group(3))
+    # both gauge-fixed: maxima of the functional near 1 (Gribov copies may differ)
+    assert 0.5 < f_fa < 1.0 and abs(f_fa - f_or) < 1e-3
