@@ -1572,11 +1572,8 @@ template <int GRP, class T, int ND> struct Ops
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
 	// packed FP32x2 products; 14-17, 21-28: thread per site
 	// (k_momentum_step_site) with FP32x2 products, tiles and launch shapes;
-	// 18-20: thread per site, plain products (every group and precision);
-	// 29: thread per site, FP32x2, 5 blocks of 128 per SM (at most 102
-	// registers a thread: one more resident warp per scheduler for fewer
-	// registers)
-	static constexpr int kForceVariants = 30;
+	// 18-20: thread per site, plain products (every group and precision)
+	static constexpr int kForceVariants = 29;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1609,8 +1606,7 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/f32x2", 1},
 		    {2, {2, 1, 1, 3}, 128, 4, "site/tile4x2x2x8/128thr/4blk/f32x2", 1},
 		    {2, {0, 0, 3, 4}, 128, 4, "site/tile1x1x8x16/128thr/4blk/f32x2", 1},
-		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1},
-		    {2, {0, 2, 2, 3}, 128, 5, "site/tile1x4x4x8/128thr/5blk/f32x2", 1}};
+		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1705,10 +1701,6 @@ template <int GRP, class T, int ND> struct Ops
 	static void site_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u, T *p,
 	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
 	{
-		if constexpr (F2 == 1)
-			if (fv.threads == 128 && fv.minb == 5)
-				return k_momentum_step_site<GRP, T, 4, 128, 5, F2, ROWS, FUSE>
-				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 		if (fv.threads == 512)
 			k_momentum_step_site<GRP, T, 4, 512, 1, F2, ROWS, FUSE>
 			    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
@@ -1740,7 +1732,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 29; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 28; // the thread-per-site variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
