@@ -587,7 +587,7 @@ template <typename F> void dispatchByGroup(F f, std::string const &group, int pr
 		else
 			throw std::runtime_error("unknown gauge group '" + group + "'");
 	}
-	else
+	else // the reference's message, verbatim (utils.h:185)
 		throw std::runtime_error("invlid precision level '" + std::to_string(precision) + "'");
 }
 

@@ -106,6 +106,53 @@ def test_cpp_dropin_app_compiles(libpath, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+DISPATCH_CPP = r"""
+#include "mesh/mesh.hpp"
+#include <cstdio>
+struct Show
+{
+	template <class G> void operator()() const
+	{
+		std::printf("%s %d %zu\n", std::string(mesh::GaugeTraits<G>::name()).c_str(),
+		            int(mesh::GaugeTraits<G>::precision), sizeof(typename mesh::GaugeTraits<G>::real));
+	}
+};
+int main()
+{
+	for (int p : {1, 2})
+		for (char const *g : {"u1", "su2", "su3"})
+			mesh::dispatchByGroup(Show{}, g, p);
+	for (auto [g, p] : {std::pair{"su4", 1}, std::pair{"su3", 3}})
+		try
+		{
+			mesh::dispatchByGroup(Show{}, g, p);
+		}
+		catch (std::runtime_error const &e)
+		{
+			std::printf("error: %s\n", e.what());
+		}
+	return 0;
+}
+"""
+
+
+def test_cpp_dispatch_by_group_without_gpu(libpath, tmp_path):
+    """dispatchByGroup (src/gauge/utils.h:156-186): the group names and
+    precision levels of the reference select the same instantiations, and
+    unknown ones raise the reference's messages"""
+    src = tmp_path / "d.cpp"
+    src.write_text(DISPATCH_CPP)
+    exe = tmp_path / "d"
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-L", os.path.dirname(libpath), "-lmesh_gb300", "-Wl,-rpath," + os.path.dirname(libpath),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout.splitlines()
+    assert out[:6] == ["u1 1 4", "su2 1 4", "su3 1 4", "u1 2 8", "su2 2 8", "su3 2 8"]
+    assert out[6] == "error: unknown gauge group 'su4'"
+    assert out[7] == "error: invlid precision level '3'"
+
+
 def test_cpp_landau_fa_instantiate(libpath, tmp_path):
     """the C++ wrapper of the Fourier-accelerated solver compiles (FP64
     groups only) and the raw FP32 copy of the committed network matches the
