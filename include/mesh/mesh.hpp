@@ -20,6 +20,8 @@
 
 #include "../mesh_gb300.h"
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -133,9 +135,19 @@ class Grid
 
 // ---- fields -------------------------------------------------------------------
 namespace detail {
+// owned fields are destroyed with their object; borrowed ones (a chain's U and P)
+// belong to the chain
 struct FieldDeleter
 {
-	void operator()(mesh_field_s *f) const { mesh_field_destroy(f); }
+	bool owned = true;
+	void operator()(mesh_field_s *f) const
+	{
+		if (owned)
+			mesh_field_destroy(f);
+	}
+};
+struct borrow_t
+{
 };
 using FieldPtr = std::unique_ptr<mesh_field_s, FieldDeleter>;
 
@@ -166,19 +178,38 @@ template <class G> class BasicField
 	    : grid_(g), nstack_(nstack), kind_(kind),
 	      h_(detail::make_field(c, kind, Traits::group, Traits::precision, g, nstack))
 	{}
+	// a view of a field owned elsewhere (Hmc<G>::U and P)
+	BasicField(Grid const &g, int nstack, int kind, mesh_field borrowed, detail::borrow_t)
+	    : grid_(g), nstack_(nstack), kind_(kind), h_(borrowed, detail::FieldDeleter{false})
+	{}
 	BasicField(BasicField const &o) : BasicField(o.grid_, o.nstack_, o.kind_) { check(mesh_field_copy(get(), o.get())); }
 	BasicField(BasicField &&) noexcept = default;
+	// assignment copies the contents (deep copy, as the reference); a borrowed
+	// field keeps its buffer, so `hmc.U = readConfig<G>(...)` sets the chain's links
 	BasicField &operator=(BasicField const &o)
 	{
 		if (this != &o)
 		{
-			if (!h_ || !(grid_ == o.grid_) || nstack_ != o.nstack_ || kind_ != o.kind_)
+			bool same = h_ && grid_ == o.grid_ && nstack_ == o.nstack_ && kind_ == o.kind_;
+			if (!same && borrowed())
+				throw std::runtime_error("mesh: a chain's field can only be assigned a field of its own shape");
+			if (!same)
 				*this = BasicField(o.grid_, o.nstack_, o.kind_);
 			check(mesh_field_copy(get(), o.get()));
 		}
 		return *this;
 	}
-	BasicField &operator=(BasicField &&) noexcept = default;
+	BasicField &operator=(BasicField &&o)
+	{
+		if (borrowed())
+			return *this = static_cast<BasicField const &>(o);
+		grid_ = std::move(o.grid_);
+		nstack_ = o.nstack_;
+		kind_ = o.kind_;
+		h_ = std::move(o.h_);
+		return *this;
+	}
+	bool borrowed() const { return h_ && !h_.get_deleter().owned; }
 
 	mesh_field get() const { return h_.get(); }
 	Grid const &grid() const { return grid_; }
@@ -229,6 +260,9 @@ template <class G> class LatticeStack : public BasicField<G>
 	LatticeStack() = default;
 	explicit LatticeStack(Grid const &g, bool algebra = false, Context &c = Context::current())
 	    : BasicField<G>(g, g.ndim(), algebra ? MESH_ALGEBRA : MESH_GROUP, c)
+	{}
+	LatticeStack(Grid const &g, bool algebra, mesh_field borrowed, detail::borrow_t b)
+	    : BasicField<G>(g, g.ndim(), algebra ? MESH_ALGEBRA : MESH_GROUP, borrowed, b)
 	{}
 	size_t ndirs() const { return size_t(this->nstack_); }
 	void set_unit() { check(mesh_field_set_unit(this->get())); }
@@ -353,19 +387,33 @@ template <class G> class Hmc
 		void operator()(mesh_hmc_s *h) const { mesh_hmc_destroy(h); }
 	};
 	std::unique_ptr<mesh_hmc_s, Del> h_;
+	static mesh_hmc create(Grid const &grid, uint64_t seed, Context &c)
+	{
+		mesh_hmc h = nullptr;
+		check(mesh_hmc_create(c.get(), GaugeTraits<G>::group, GaugeTraits<G>::precision, grid.ndim(),
+		                      grid.shape().data(), seed, &h));
+		return h;
+	}
+	static mesh_field state(mesh_hmc h, int which)
+	{
+		mesh_field f = nullptr;
+		check(mesh_hmc_field(h, which, &f));
+		return f;
+	}
+	uint64_t momentum_draws_ = 0;
 
   public:
 	Grid const &g;
 	uint64_t seed;
+	// the chain's gauge field and momenta (hmc.h:71-72): views of its device
+	// fields; assigning to U (e.g. U = readConfig<G>(path)) sets the chain's links
+	GaugeField<G> U, P;
 	std::vector<double> plaq_history, deltaH_history, accept_history, time_history;
 
-	explicit Hmc(Grid const &grid, uint64_t seed_ = 0, Context &c = Context::current()) : g(grid), seed(seed_)
-	{
-		mesh_hmc h = nullptr;
-		check(mesh_hmc_create(c.get(), GaugeTraits<G>::group, GaugeTraits<G>::precision, grid.ndim(),
-		                      grid.shape().data(), seed_, &h));
-		h_.reset(h);
-	}
+	explicit Hmc(Grid const &grid, uint64_t seed_ = 0, Context &c = Context::current())
+	    : h_(create(grid, seed_, c)), g(grid), seed(seed_), U(grid, false, state(h_.get(), 0), detail::borrow_t{}),
+	      P(grid, true, state(h_.get(), 1), detail::borrow_t{})
+	{}
 	mesh_hmc get() const { return h_.get(); }
 	// the gauge field and momenta in the reference's host layout
 	std::vector<G> U_to_host() const
@@ -390,18 +438,26 @@ template <class G> class Hmc
 		time_history.clear();
 	}
 	void randomizeGaugeField() { check(mesh_hmc_randomize(get())); }
+	// new Gaussian momenta in P (hmc.cpp:65-74); runHmcUpdate draws its own, as
+	// the reference's does, from the trajectory's stream
+	void randomizeMomenta() { random_algebra_field(P, seed, (uint64_t(1) << 40) + momentum_draws_++); }
 	void coldStart() { check(mesh_hmc_cold_start(get())); }
 	// checkpoint / resume (links, trajectory counter, seed)
 	void save(std::string const &path) const { check(mesh_hmc_save(get(), path.c_str())); }
 	void load(std::string const &path) { check(mesh_hmc_load(get(), path.c_str())); }
 	// generate momenta -> run a trajectory -> accept/reject -> measure
+	// (hmc.cpp:76-107; the action of U is recomputed every trajectory, as there,
+	// since U may have been written through the view)
 	void runHmcUpdate(double beta, std::vector<double> const &deltas)
 	{
+		auto t0 = std::chrono::steady_clock::now();
+		state(get(), 0); // marks the chain's cached action of U stale
 		mesh_hmc_record r{};
 		check(mesh_hmc_update(get(), beta, deltas.data(), int(deltas.size()), &r));
 		plaq_history.push_back(r.plaquette);
 		deltaH_history.push_back(r.dH);
 		accept_history.push_back(r.accept);
+		time_history.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
 	}
 	void print_summary() const
 	{
@@ -418,6 +474,10 @@ template <class G> class Hmc
 			var += (x - m) * (x - m);
 		var = plaq_history.size() > 1 ? var / double(plaq_history.size() - 1) : 0.0;
 		std::printf("========== HMC summary ==========\n");
+		if (!time_history.empty())
+			std::printf("time per step = %.3f s (min = %.3f, max = %.3f)\n", mean(time_history, id),
+			            *std::min_element(time_history.begin(), time_history.end()),
+			            *std::max_element(time_history.begin(), time_history.end()));
 		std::printf("plaquette = %.4f +- %.4f\n", m, std::sqrt(var / double(plaq_history.size())));
 		std::printf("acceptance = %.2f\n", mean(accept_history, id));
 		std::printf("<exp(-dH)> = %.4f\n", mean(deltaH_history, [](double x) { return std::exp(-x); }));

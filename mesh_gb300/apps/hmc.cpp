@@ -6,6 +6,8 @@
 //       -L mesh_gb300 -lmesh_gb300 -Wl,-rpath,$PWD/mesh_gb300 -o hmc
 //   ./hmc --group su3 --geom 8 8 8 8 --beta 5.7 --start cold --scheme 2lf
 //         --epsilon 0.5 --substeps 10 --count 20 --seed 1234 --precision 2
+//         (--start random | cold | FILE: a configuration file, as the reference's
+//          hmc.U = readConfig<G>(start, &g))
 //         [--checkpoint chain.bin]   links + trajectory counter at the end
 //         [--resume chain.bin]       continue a chain (same --seed) from a checkpoint
 #include "mesh/mesh.hpp"
@@ -85,7 +87,7 @@ int main(int argc, char **argv)
 			    else if (start == "cold")
 				    hmc.coldStart();
 			    else
-				    throw std::runtime_error("start must be 'random' or 'cold'");
+				    hmc.U = readConfig<G>(start, &g);
 			    auto t0 = std::chrono::steady_clock::now();
 			    for (int iter = 0; iter < count; ++iter)
 				    hmc.runHmcUpdate(beta, deltas);

@@ -46,6 +46,14 @@ def test_app_matches_oracle_and_resumes(oracle, tmp_path):
     first = run(exe, *common, "--start", "cold", "--count", "3", "--checkpoint", ck)
     second = run(exe, *common, "--resume", ck, "--count", "3")
     np.testing.assert_array_equal(np.vstack([first, second]), full)
+    # --start FILE (the reference's hmc.U = readConfig<G>(start, &g)): a new
+    # chain, trajectory counter 0, from the checkpointed links
+    from_file = run(exe, *common, "--start", ck, "--count", "2")
+    deltas = oracle.make_deltas("2lf", 0.5, 10)
+    U3, _ = oracle.hmc_chain(3, 2, dims, oracle.unit_gauge(3, 2, dims), 5.7, deltas, 1234, 0, 3)
+    _, recs2 = oracle.hmc_chain(3, 2, dims, U3, 5.7, deltas, 1234, 0, 2)
+    np.testing.assert_array_equal(from_file[:, 2], recs2[:, 2])
+    np.testing.assert_allclose(from_file[:, 0], recs2[:, 0], rtol=1e-10)
 
 
 LANDAU_FA_CPP = r"""
