@@ -32,6 +32,7 @@
 #include <string>
 #include <string_view>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 namespace mesh {
@@ -300,6 +301,42 @@ template <class G> double norm2(BasicField<G> const &a)
 	double s = 0;
 	check(mesh_field_norm2(a.get(), &s));
 	return s;
+}
+
+// linear operations on Lattice<G> and GaugeField<G> (MESH_DEFINE_LATTICE_BINARY
+// +, -, lattice.h:289-334; operator*(Lattice, double), lattice.h:348-356;
+// add_mul, lattice.h:358-364): a new field of the operands' shape, or in place
+template <class L>
+concept MeshField = std::is_base_of_v<BasicField<typename L::value_type>, L>;
+template <MeshField L> L axpby(double a, L const &x, double b, L const *y)
+{
+	L r(x.grid(), x.is_algebra());
+	check(mesh_field_axpby(r.get(), a, x.get(), b, y ? y->get() : nullptr));
+	return r;
+}
+template <MeshField L> L operator+(L const &x, L const &y) { return axpby(1.0, x, 1.0, &y); }
+template <MeshField L> L operator-(L const &x, L const &y) { return axpby(1.0, x, -1.0, &y); }
+template <MeshField L> L operator*(L const &x, double s) { return axpby<L>(s, x, 0.0, nullptr); }
+template <MeshField L> L operator*(double s, L const &x) { return axpby<L>(s, x, 0.0, nullptr); }
+template <MeshField L> L &operator+=(L &x, L const &y)
+{
+	check(mesh_field_axpby(x.get(), 1.0, x.get(), 1.0, y.get()));
+	return x;
+}
+template <MeshField L> L &operator-=(L &x, L const &y)
+{
+	check(mesh_field_axpby(x.get(), 1.0, x.get(), -1.0, y.get()));
+	return x;
+}
+template <MeshField L> L &operator*=(L &x, double s)
+{
+	check(mesh_field_axpby(x.get(), s, x.get(), 0.0, nullptr));
+	return x;
+}
+// lhs += m * rhs for a real m
+template <MeshField L> void add_mul(L &lhs, double m, L const &rhs)
+{
+	check(mesh_field_axpby(lhs.get(), 1.0, lhs.get(), m, rhs.get()));
 }
 
 // ---- gauge utilities (utils.h) -------------------------------------------------

@@ -140,6 +140,13 @@ void *mesh_field_device_ptr(mesh_field f);
 int mesh_site_cshift(mesh_field dst, mesh_field src, int dir, int offset);
 /* dst = a * b (MESH_DEFINE_LATTICE_BINARY(*), lattice.h:289-301) */
 int mesh_site_mul(mesh_field dst, mesh_field a, mesh_field b);
+/* out = a x + b y object by object, for fields of one shape (any kind and
+ * stack size); y may be NULL (out = a x), out may be x or y. Every field kind
+ * stores its objects linearly (matrices, quaternions, complex numbers, packed
+ * algebra), so this is the reference's lattice +, -, scalar * and their
+ * compound forms (MESH_DEFINE_LATTICE_BINARY, lattice.h:289-334;
+ * operator*(Lattice, double), lattice.h:348-356) and add_mul (lattice.h:358-364) */
+int mesh_field_axpby(mesh_field out, double a, mesh_field x, double b, mesh_field y);
 /* dst = adj(a) (utils.h:31) */
 int mesh_site_adj(mesh_field dst, mesh_field a);
 /* sum_x real_trace(a(x)) in FP64 (sum_real_trace, utils.h:29) */

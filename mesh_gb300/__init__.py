@@ -86,6 +86,7 @@ SIGNATURES = {
     "mesh_site_cshift": (_I, [_P, _P, _I, _I]),
     "mesh_site_mul": (_I, [_P, _P, _P]),
     "mesh_site_adj": (_I, [_P, _P]),
+    "mesh_field_axpby": (_I, [_P, _D, _P, _D, _P]),
     "mesh_site_sum_real_trace": (_I, [_P, _DP]),
     "mesh_field_norm2": (_I, [_P, _DP]),
     "mesh_plaquette": (_I, [_P, _DP]),
@@ -394,6 +395,12 @@ def cshift(dst: Field, src: Field, dir: int, offset: int) -> Field:
 def site_mul(dst: Field, a: Field, b: Field) -> Field:
     _chk(load().mesh_site_mul(dst.h, a.h, b.h))
     return dst
+
+
+def axpby(out: Field, a: float, x: Field, b: float = 0.0, y: Field = None) -> Field:
+    """out = a x + b y object by object (y optional; out may be x or y)"""
+    _chk(load().mesh_field_axpby(out.h, a, x.h, b, y.h if y is not None else None))
+    return out
 
 
 def site_adj(dst: Field, a: Field) -> Field:

@@ -224,6 +224,16 @@ void check_deltas(double const *deltas, int n)
 	require(n % 2 == 1, "step table must alternate position/momentum steps and have odd length");
 }
 
+// out = a x + b y over every stored real, y optional; out may be x or y (no
+// restrict). One thread per real in a grid-stride loop: consecutive threads
+// read consecutive words of each array.
+template <class T>
+__global__ void __launch_bounds__(256) k_axpby(int64_t n, T a, T const *x, T b, T const *y, T *out)
+{
+	for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+		out[i] = y ? a * x[i] + b * y[i] : a * x[i];
+}
+
 } // namespace
 
 void meshgb::ctx_retain(Context &c) { ++c.refs; }
@@ -606,6 +616,35 @@ int mesh_site_mul(mesh_field dst, mesh_field a, mesh_field b)
 		        "site_mul operates on single-component group fields");
 		DeviceGuard dg(d.ctx->device);
 		ops_for(d).site_op(SITE_MUL, d, x, &y);
+	});
+}
+
+int mesh_field_axpby(mesh_field out, double a, mesh_field x, double b, mesh_field y)
+{
+	return api([&] {
+		require(out != nullptr && x != nullptr, "null field");
+		Field &o = F(out), &u = F(x);
+		same_shape(o, u);
+		require(o.kind == u.kind && o.nstack == u.nstack, "fields differ in kind or stack size", MESH_ERR_STATE);
+		Field *v = y ? &F(y) : nullptr;
+		if (v)
+		{
+			same_shape(o, *v);
+			require(o.kind == v->kind && o.nstack == v->nstack, "fields differ in kind or stack size", MESH_ERR_STATE);
+		}
+		int64_t n = int64_t(o.bytes / o.real_bytes);
+		Context &c = *o.ctx;
+		DeviceGuard dg(c.device);
+		unsigned blocks = grid_for(c, n, 256);
+		if (o.prec == MESH_F32)
+			k_axpby<float><<<blocks, 256, 0, c.stream>>>(n, float(a), static_cast<float const *>(u.d), float(b),
+			                                             v ? static_cast<float const *>(v->d) : nullptr,
+			                                             static_cast<float *>(o.d));
+		else
+			k_axpby<double><<<blocks, 256, 0, c.stream>>>(n, a, static_cast<double const *>(u.d), b,
+			                                              v ? static_cast<double const *>(v->d) : nullptr,
+			                                              static_cast<double *>(o.d));
+		MESH_LAUNCH_CHECK();
 	});
 }
 

@@ -163,6 +163,11 @@ def test_cpp_landau_fa_instantiate(libpath, tmp_path):
     src.write_text('#include "mesh/mesh.hpp"\n'
                    "template class mesh::LandauFA<mesh::SU3<double>>;\n"
                    "template class mesh::LandauFA<mesh::U1<double>>;\n"
+                   "auto lin(mesh::Lattice<mesh::SU3<float>> const &a, mesh::Lattice<mesh::SU3<float>> const &b)\n"
+                   "{ auto c = a + b; c -= a; c *= 2.0; c += b; mesh::add_mul(c, 0.5, b);\n"
+                   "  return 3.0 * (c - b) * 1.0 * (a * b); }\n"
+                   "auto lin2(mesh::GaugeField<mesh::U1<double>> &U, mesh::GaugeField<mesh::U1<double>> const &P)\n"
+                   "{ U += 0.5 * P; mesh::add_mul(U, -1.0, P); return U - P; }\n"
                    "std::vector<float> f() { return mesh::readMlpParams(\"x.f32\"); }\n")
     r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Werror", "-c", "-I", os.path.join(ROOT, "include"),
                         str(src), "-o", str(tmp_path / "fa.o")], capture_output=True, text=True)

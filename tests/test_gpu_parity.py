@@ -129,6 +129,37 @@ def test_cshift_mul_adj_sum_vs_oracle(ctx, oracle, g, p):
                                                  rel=1e-12 if p == 2 else 1e-5, abs=1e-9 if p == 2 else 1e-3)
 
 
+@pytest.mark.parametrize("algebra", [False, True])
+@pytest.mark.parametrize("g,p", CASES)
+def test_linear_combinations_vs_host(ctx, oracle, g, p, algebra):
+    """out = a x + b y (mesh_field_axpby: the reference's lattice +, -,
+    scalar * and add_mul, lattice.h:289-364) on gauge fields and momenta of
+    every group: exported, it is the same combination of the exported
+    operands (import and export are linear maps); also without y and in place
+    (out = x). FP64 to 1e-15, FP32 to 1e-6 relative."""
+    dims = [4, 6, 2, 4]
+    grid = mg.Grid(dims)
+    if algebra:
+        xh, yh = oracle.random_momenta(g, p, dims, 5, 0), oracle.random_momenta(g, p, dims, 6, 0)
+        make = mg.Momenta
+    else:
+        xh, yh = oracle.random_gauge(g, p, dims, 5), oracle.random_gauge(g, p, dims, 6)
+        make = mg.GaugeField
+    x = make(ctx, g, p, grid).import_(xh)
+    y = make(ctx, g, p, grid).import_(yh)
+    out = make(ctx, g, p, grid)
+    X, Y = xh.astype(np.float64), yh.astype(np.float64)
+    t = 1e-15 if p == 2 else 1e-6
+    mg.axpby(out, 0.75, x, -1.5, y)
+    assert rel(out.export(), 0.75 * X - 1.5 * Y) < t
+    mg.axpby(out, 2.0, x)
+    assert rel(out.export(), 2.0 * X) < t
+    mg.axpby(x, 1.0, x, 0.5, y)
+    assert rel(x.export(), X + 0.5 * Y) < t
+    with pytest.raises(mg.MeshError):
+        mg.axpby(out, 1.0, mg.Lattice(ctx, g, p, grid), 1.0, y)
+
+
 # ---------------------------------------------------------------------------
 # gauge kernels
 # ---------------------------------------------------------------------------
