@@ -290,6 +290,20 @@ template <class G> Lattice<G> adj(Lattice<G> const &a)
 	check(mesh_site_adj(r.get(), a.get()));
 	return r;
 }
+// exp of an algebra field, and the algebra projection of a group-type field
+// (MESH_DEFINE_LATTICE_UNARY(exp / project_on_algebra), utils.h:32-33)
+template <class G> Lattice<G> exp(Lattice<G> const &a)
+{
+	Lattice<G> r(a.grid());
+	check(mesh_site_exp(r.get(), a.get()));
+	return r;
+}
+template <class G> Lattice<G> project_on_algebra(Lattice<G> const &a)
+{
+	Lattice<G> r(a.grid(), true);
+	check(mesh_site_project(r.get(), a.get()));
+	return r;
+}
 template <class G> double sum_real_trace(Lattice<G> const &a)
 {
 	double s = 0;

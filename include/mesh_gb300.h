@@ -147,6 +147,13 @@ int mesh_site_mul(mesh_field dst, mesh_field a, mesh_field b);
  * compound forms (MESH_DEFINE_LATTICE_BINARY, lattice.h:289-334;
  * operator*(Lattice, double), lattice.h:348-356) and add_mul (lattice.h:358-364) */
 int mesh_field_axpby(mesh_field out, double a, mesh_field x, double b, mesh_field y);
+/* dst = exp(a), a an algebra field, dst a group field
+ * (MESH_DEFINE_LATTICE_UNARY(exp, gauge::exp), utils.h:32) */
+int mesh_site_exp(mesh_field dst, mesh_field a);
+/* dst = project_on_algebra(a): the antihermitian traceless part of the
+ * group-type objects of a, into an algebra field (utils.h:33;
+ * groups.h:64-67,142-145,224-228) */
+int mesh_site_project(mesh_field dst, mesh_field a);
 /* dst = adj(a) (utils.h:31) */
 int mesh_site_adj(mesh_field dst, mesh_field a);
 /* sum_x real_trace(a(x)) in FP64 (sum_real_trace, utils.h:29) */

@@ -87,6 +87,8 @@ SIGNATURES = {
     "mesh_site_mul": (_I, [_P, _P, _P]),
     "mesh_site_adj": (_I, [_P, _P]),
     "mesh_field_axpby": (_I, [_P, _D, _P, _D, _P]),
+    "mesh_site_exp": (_I, [_P, _P]),
+    "mesh_site_project": (_I, [_P, _P]),
     "mesh_site_sum_real_trace": (_I, [_P, _DP]),
     "mesh_field_norm2": (_I, [_P, _DP]),
     "mesh_plaquette": (_I, [_P, _DP]),
@@ -401,6 +403,18 @@ def axpby(out: Field, a: float, x: Field, b: float = 0.0, y: Field = None) -> Fi
     """out = a x + b y object by object (y optional; out may be x or y)"""
     _chk(load().mesh_field_axpby(out.h, a, x.h, b, y.h if y is not None else None))
     return out
+
+
+def site_exp(dst: Field, a: Field) -> Field:
+    """dst (group) = exp(a) for an algebra field a"""
+    _chk(load().mesh_site_exp(dst.h, a.h))
+    return dst
+
+
+def site_project(dst: Field, a: Field) -> Field:
+    """dst (algebra) = project_on_algebra(a) for a group-type field a"""
+    _chk(load().mesh_site_project(dst.h, a.h))
+    return dst
 
 
 def site_adj(dst: Field, a: Field) -> Field:

@@ -648,6 +648,30 @@ int mesh_field_axpby(mesh_field out, double a, mesh_field x, double b, mesh_fiel
 	});
 }
 
+int mesh_site_exp(mesh_field dst, mesh_field a)
+{
+	return api([&] {
+		Field &d = F(dst), &x = F(a);
+		same_shape(d, x);
+		require(d.kind == MESH_GROUP && x.kind == MESH_ALGEBRA && d.nstack == 1 && x.nstack == 1,
+		        "site_exp maps a single-component algebra field to a group field");
+		DeviceGuard dg(d.ctx->device);
+		ops_for(d).site_op(SITE_EXP, d, x, nullptr);
+	});
+}
+
+int mesh_site_project(mesh_field dst, mesh_field a)
+{
+	return api([&] {
+		Field &d = F(dst), &x = F(a);
+		same_shape(d, x);
+		require(d.kind == MESH_ALGEBRA && x.kind == MESH_GROUP && d.nstack == 1 && x.nstack == 1,
+		        "site_project maps a single-component group field to an algebra field");
+		DeviceGuard dg(d.ctx->device);
+		ops_for(d).site_op(SITE_PROJ, d, x, nullptr);
+	});
+}
+
 int mesh_site_adj(mesh_field dst, mesh_field a)
 {
 	return api([&] {

@@ -64,6 +64,8 @@ enum SiteOp
 	SITE_MUL = 0,
 	SITE_ADJ = 1,
 	SITE_COPY = 2,
+	SITE_EXP = 3,  // group dst = exp(algebra a)
+	SITE_PROJ = 4, // algebra dst = antihermitian traceless part of group-type a
 };
 
 // Scalar-producing reduction slots (indices into the context's slots)

@@ -347,7 +347,22 @@ __global__ void __launch_bounds__(kBlock)
 	MESH_GRID_LOOP(s, V)
 	{
 		E x, y, r;
+		if (op == SITE_EXP) // a holds packed algebra elements
+		{
+			T o[Gp::NA];
+			Soa<T, Gp::NA>::load(a, V, s, o);
+			r = Gp::exp_alg(o, T(1));
+			Soa<T, Gp::NR>::store(dst, V, s, r.v);
+			continue;
+		}
 		Soa<T, Gp::NR>::load(a, V, s, x.v);
+		if (op == SITE_PROJ) // dst holds packed algebra elements
+		{
+			T o[Gp::NA];
+			Gp::proj(x, o);
+			Soa<T, Gp::NA>::store(dst, V, s, o);
+			continue;
+		}
 		if (op == SITE_MUL)
 		{
 			Soa<T, Gp::NR>::load(b, V, s, y.v);

@@ -165,7 +165,7 @@ def test_cpp_landau_fa_instantiate(libpath, tmp_path):
                    "template class mesh::LandauFA<mesh::U1<double>>;\n"
                    "auto lin(mesh::Lattice<mesh::SU3<float>> const &a, mesh::Lattice<mesh::SU3<float>> const &b)\n"
                    "{ auto c = a + b; c -= a; c *= 2.0; c += b; mesh::add_mul(c, 0.5, b);\n"
-                   "  return 3.0 * (c - b) * 1.0 * (a * b); }\n"
+                   "  return 3.0 * (c - b) * 1.0 * (a * b) * mesh::exp(mesh::project_on_algebra(a)); }\n"
                    "auto lin2(mesh::GaugeField<mesh::U1<double>> &U, mesh::GaugeField<mesh::U1<double>> const &P)\n"
                    "{ U += 0.5 * P; mesh::add_mul(U, -1.0, P); return U - P; }\n"
                    "std::vector<float> f() { return mesh::readMlpParams(\"x.f32\"); }\n")

@@ -129,6 +129,44 @@ def test_cshift_mul_adj_sum_vs_oracle(ctx, oracle, g, p):
                                                  rel=1e-12 if p == 2 else 1e-5, abs=1e-9 if p == 2 else 1e-3)
 
 
+def np_project_on_algebra(g, a):
+    """project_on_algebra (groups.h:64-67,142-145,224-228) on host-layout
+    objects: U(1) (re, im) -> (0, im); SU(2) quaternions (re, im1, im2, im3)
+    -> (0, im1, im2, im3); SU(3) row-major complex 3x3 -> (A - A^+)/2 minus
+    its trace part"""
+    a = np.asarray(a, dtype=np.float64)
+    r = a.copy()
+    if g in (1, 2):
+        r[..., 0] = 0.0
+        return r
+    m = (a[..., 0::2] + 1j * a[..., 1::2]).reshape(*a.shape[:-1], 3, 3)
+    h = 0.5 * (m - np.conj(np.swapaxes(m, -1, -2)))
+    h -= np.trace(h, axis1=-2, axis2=-1)[..., None, None] / 3.0 * np.eye(3)
+    h = h.reshape(*a.shape[:-1], 9)
+    r[..., 0::2], r[..., 1::2] = h.real, h.imag
+    return r
+
+
+@pytest.mark.parametrize("g,p", CASES)
+def test_site_exp_and_project_vs_oracle(ctx, oracle, g, p):
+    """exp of an algebra field (utils.h:32) against the oracle's evolve of
+    unit links by t = 1, and project_on_algebra of a group field (utils.h:33)
+    against its restatement on the host objects"""
+    dims = [4, 6, 2, 4]
+    grid = mg.Grid(dims)
+    P = oracle.random_momenta(g, p, dims, 7, 0)
+    U = oracle.random_gauge(g, p, dims, 8)
+    a = mg.Lattice(ctx, g, p, grid, algebra=True).import_(P[0])
+    e = mg.site_exp(mg.Lattice(ctx, g, p, grid), a)
+    ref = oracle.evolve(g, 2, dims, oracle.unit_gauge(g, 2, dims), P.astype(np.float64), 1.0)[0]
+    assert rel(e.export(), ref) < tol(p)
+    u = mg.Lattice(ctx, g, p, grid).import_(U[0])
+    pr = mg.site_project(mg.Lattice(ctx, g, p, grid, algebra=True), u)
+    assert rel(pr.export(), np_project_on_algebra(g, U[0])) < (1e-15 if p == 2 else 1e-6)
+    with pytest.raises(mg.MeshError):
+        mg.site_exp(mg.Lattice(ctx, g, p, grid), u)
+
+
 @pytest.mark.parametrize("algebra", [False, True])
 @pytest.mark.parametrize("g,p", CASES)
 def test_linear_combinations_vs_host(ctx, oracle, g, p, algebra):
