@@ -571,11 +571,20 @@ template <class G> struct Landau
 
 	explicit Landau(GaugeField<G> const &U_) : U(U_), g(Lattice<G>::identity(U_.grid())) {}
 	void reset() { check(mesh_field_set_unit(g.get())); }
-	double operator()() const
+	// the functional at the transform h (landau.h:23-32), or at g
+	double operator()(Lattice<G> const &h) const
 	{
 		double s = 0;
-		check(mesh_landau_functional(U.get(), g.get(), &s));
+		check(mesh_landau_functional(U.get(), h.get(), &s));
 		return s;
+	}
+	double operator()() const { return (*this)(g); }
+	// the step along the algebra field F from g that run() takes (landau.h:77-98)
+	double line_search(Lattice<G> const &F, double eps) const
+	{
+		double step = 0;
+		check(mesh_landau_line_search(U.get(), g.get(), F.get(), eps, &step));
+		return step;
 	}
 	double condition() const
 	{

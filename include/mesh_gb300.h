@@ -332,6 +332,11 @@ int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_del
 /* functional sum_mu sum_x ReTr(g(x) U_mu(x) g(x+mu)^dagger)/(Nc Nd V)
  * (Landau::operator(), landau.h:23-32), FP64 */
 int mesh_landau_functional(mesh_field U, mesh_field g, double *out);
+/* Landau::line_search (landau.h:77-98): the step along the algebra field F
+ * (single component) from g that mesh_landau_cg takes (halving eps until
+ * the functional rises, then the quadratic model through eps, 1.2 eps,
+ * 0.8 eps; 0 when eps falls below 1e-10) */
+int mesh_landau_line_search(mesh_field U, mesh_field g, mesh_field F, double eps, double *step);
 /* theta_ref = sum_x |Delta(x)|^2 / (Nd V), Delta = sum_mu A_mu(x)-A_mu(x-mu)
  * (Landau::condition, landau.h:37-49), FP64 */
 int mesh_landau_theta(mesh_field U, mesh_field g, double *out);

@@ -128,6 +128,7 @@ SIGNATURES = {
     "mesh_batch_plaquettes": (_I, [_P, _DP]),
     "mesh_batch_launch_info": (_I, [_P, _IP, _I, _IP, _IP]),
     "mesh_landau_functional": (_I, [_P, _P, _DP]),
+    "mesh_landau_line_search": (_I, [_P, _P, _P, _D, _DP]),
     "mesh_landau_theta": (_I, [_P, _P, _DP]),
     "mesh_landau_deriv": (_I, [_P, _P, _P]),
     "mesh_landau_cg": (_I, [_P, _P, _I, _D, _IP, _DP]),
@@ -708,9 +709,16 @@ class Landau:
     def reset(self):
         self.g.set_unit()
 
-    def __call__(self) -> float:
+    def __call__(self, h: Field = None) -> float:
+        """the functional at g, or at the transform h (landau.h:23-34)"""
         out = C.c_double()
-        _chk(load().mesh_landau_functional(self.U.h, self.g.h, C.byref(out)))
+        _chk(load().mesh_landau_functional(self.U.h, (self.g if h is None else h).h, C.byref(out)))
+        return out.value
+
+    def line_search(self, F: Field, eps: float) -> float:
+        """the CG's step along the algebra field F from g (landau.h:77-98)"""
+        out = C.c_double()
+        _chk(load().mesh_landau_line_search(self.U.h, self.g.h, F.h, eps, C.byref(out)))
         return out.value
 
     def condition(self) -> float:

@@ -1287,6 +1287,62 @@ int mesh_landau_deriv(mesh_field Fh, mesh_field Uh, mesh_field gh)
 	});
 }
 
+// Landau::line_search (landau.h:77-98): the step along the algebra field Fd
+// from g that the three-point quadratic model of the functional puts at its
+// maximum (after halving eps until the functional rises; 0 below 1e-10);
+// gt is scratch for exp(eps Fd) g
+static double landau_line_search(Field const &U, Field const &g, Field const &Fd, Field &gt, double eps)
+{
+	Context &c = *U.ctx;
+	auto const &ops = ops_for(U);
+	double norm_fac = 1.0 / (double(group_nc(U.group)) * U.nd * double(U.geom.V));
+	auto functional = [&](Field const &h) {
+		ops.landau_functional(U, h, slot(c, SLOT_TMP));
+		return read_slot(c, SLOT_TMP) * norm_fac;
+	};
+	auto stepped = [&](double e) {
+		ops.exp_apply(gt, Fd, e, g);
+		return functional(gt);
+	};
+	double base = functional(g);
+	double y1 = stepped(eps);
+	while (y1 <= base)
+	{
+		eps *= 0.5;
+		y1 = stepped(eps);
+		if (eps < 1e-10)
+			return 0.0;
+	}
+	double y2 = stepped(eps * 1.2);
+	if (y2 > y1)
+		return 1.2 * eps;
+	double y3 = stepped(eps * 0.8);
+	double x1 = eps, x2 = 1.2 * eps, x3 = 0.8 * eps;
+	return 0.5 * ((x2 * x2 - x3 * x3) * y1 - (x1 * x1 - x3 * x3) * y2 + (x1 * x1 - x2 * x2) * y3) /
+	       ((x2 - x3) * y1 - (x1 - x3) * y2 + (x1 - x2) * y3);
+}
+
+int mesh_landau_line_search(mesh_field Uh, mesh_field gh, mesh_field Fh, double eps, double *step)
+{
+	return api([&] {
+		Field &U = F(Uh), &g = F(gh), &Fd = F(Fh);
+		check_landau(U, g);
+		require(Fd.kind == MESH_ALGEBRA && Fd.nstack == 1, "F must be a single-component algebra field");
+		same_shape(U, Fd);
+		require(step != nullptr && eps > 0, "invalid argument");
+		Context &c = *U.ctx;
+		DeviceGuard dg(c.device);
+		Field gt;
+		struct Cleanup
+		{
+			Field *a;
+			~Cleanup() { destroy_field(*a); }
+		} cleanup{&gt};
+		create_field(c, MESH_GROUP, U.group, U.prec, U.nd, U.dims, 1, gt);
+		*step = landau_line_search(U, g, Fd, gt, eps);
+	});
+}
+
 int mesh_landau_cg(mesh_field Uh, mesh_field gh, int max_iter, double tol, int *iters, double *theta)
 {
 	return api([&] {
@@ -1312,33 +1368,6 @@ int mesh_landau_cg(mesh_field Uh, mesh_field gh, int max_iter, double tol, int *
 		create_field(c, MESH_GROUP, U.group, U.prec, U.nd, U.dims, 1, gt);
 		MESH_CUDA(cudaMemsetAsync(last.d, 0, last.bytes, c.stream));
 		double norm_fac = 1.0 / (double(group_nc(U.group)) * U.nd * double(U.geom.V));
-		auto functional = [&](Field const &h) {
-			ops.landau_functional(U, h, slot(c, SLOT_TMP));
-			return read_slot(c, SLOT_TMP) * norm_fac;
-		};
-		auto stepped = [&](double eps) {
-			ops.exp_apply(gt, Fd, eps, g);
-			return functional(gt);
-		};
-		// Landau::line_search (landau.h:77-98)
-		auto line_search = [&](double eps) {
-			double base = functional(g);
-			double y1 = stepped(eps);
-			while (y1 <= base)
-			{
-				eps *= 0.5;
-				y1 = stepped(eps);
-				if (eps < 1e-10)
-					return 0.0;
-			}
-			double y2 = stepped(eps * 1.2);
-			if (y2 > y1)
-				return 1.2 * eps;
-			double y3 = stepped(eps * 0.8);
-			double x1 = eps, x2 = 1.2 * eps, x3 = 0.8 * eps;
-			return 0.5 * ((x2 * x2 - x3 * x3) * y1 - (x1 * x1 - x3 * x3) * y2 + (x1 * x1 - x2 * x2) * y3) /
-			       ((x2 - x3) * y1 - (x1 - x3) * y2 + (x1 - x2) * y3);
-		};
 		double eps = 3000.0, lastNorm = 0.0, th = 0.0;
 		int it = 0;
 		bool converged = false;
@@ -1361,7 +1390,7 @@ int mesh_landau_cg(mesh_field Uh, mesh_field gh, int max_iter, double tol, int *
 			// landau.h:126-128: `last = F; F += last * beta` (last already equals F)
 			if (it > 20 && beta > 0)
 				ops.axpy_alg(Fd, beta, last);
-			eps = line_search(eps);
+			eps = landau_line_search(U, g, Fd, gt, eps);
 			ops.exp_apply(gt, Fd, eps, g);
 			MESH_CUDA(cudaMemcpyAsync(g.d, gt.d, g.bytes, cudaMemcpyDeviceToDevice, c.stream));
 			ops.reunitize(g);

@@ -163,6 +163,7 @@ def test_cpp_landau_fa_instantiate(libpath, tmp_path):
     src.write_text('#include "mesh/mesh.hpp"\n'
                    "template class mesh::LandauFA<mesh::SU3<double>>;\n"
                    "template class mesh::LandauFA<mesh::U1<double>>;\n"
+                   "template struct mesh::Landau<mesh::SU3<float>>;\n"
                    "auto lin(mesh::Lattice<mesh::SU3<float>> const &a, mesh::Lattice<mesh::SU3<float>> const &b)\n"
                    "{ auto c = a + b; c -= a; c *= 2.0; c += b; mesh::add_mul(c, 0.5, b);\n"
                    "  return 3.0 * (c - b) * 1.0 * (a * b) * mesh::exp(mesh::project_on_algebra(a)); }\n"

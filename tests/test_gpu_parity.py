@@ -535,6 +535,26 @@ def test_landau_cg_matches_oracle(ctx, oracle, g):
     assert rel(L.g.export(), go) < 1e-9
 
 
+@pytest.mark.parametrize("g", [1, 3])
+def test_landau_line_search_is_the_cg_step(ctx, oracle, g):
+    """Landau::line_search (landau.h:77-98) through its own entry point: the
+    first CG iteration from g = 1 is g <- reunit(exp(s F) g) with F = deriv()
+    and s = line_search(F, 3000), and the functional rises along it"""
+    dims = [4, 4, 4, 8]
+    grid = mg.Grid(dims)
+    U = gauge(ctx, g, 2, dims, thermal(oracle, g, dims))
+    L = mg.Landau(U)
+    F = L.deriv()
+    s = L.line_search(F, 3000.0)
+    assert s > 0
+    X = mg.axpby(mg.Lattice(ctx, g, 2, grid, algebra=True), s, F)
+    h = mg.site_mul(mg.Lattice(ctx, g, 2, grid), mg.site_exp(mg.Lattice(ctx, g, 2, grid), X), L.g)
+    assert L(h) > L()
+    mg.reunitize(h)
+    L.run(1, tol=1e-30)
+    assert rel(L.g.export(), h.export()) < 1e-12
+
+
 def test_errors_are_status_codes(ctx):
     a = mg.GaugeField(ctx, 3, 2, mg.Grid([4, 4, 4, 4]))
     b = mg.GaugeField(ctx, 3, 2, mg.Grid([4, 4, 4, 6]))
