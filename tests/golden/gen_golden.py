@@ -57,7 +57,7 @@ CASES = [
 
 def main():
     for name, grp, dims, beta in CASES:
-        rng = np.random.default_rng(abs(hash(name)) % (2**32) if False else sum(map(ord, name)))
+        rng = np.random.default_rng(sum(map(ord, name)))
         nd, V = len(dims), int(np.prod(dims))
         U = haar(grp, nd * V, rng).reshape(nd, V, NREAL[grp]).astype(np.float64)
         normals = rng.standard_normal(nd * V * NNORM[grp])

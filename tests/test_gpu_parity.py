@@ -435,7 +435,6 @@ def test_landau_pieces_vs_oracle(ctx, oracle, g, p):
     if p == 2:
         L.overrelax(1.7, tol=0.0, max_sweeps=3, check_every=3)
         ref = oracle.landau_or_sweeps(g, 2, dims, U64, h64, 1.7, 3)
-        ref = oracle.reunitize(g, 2, dims, ref[None])[0] if False else ref
         assert rel(L.g.export(), ref) < 1e-11
 
 
