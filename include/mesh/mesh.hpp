@@ -318,7 +318,7 @@ template <class G> double norm2(BasicField<G> const &a)
 }
 
 // linear operations on Lattice<G> and GaugeField<G> (MESH_DEFINE_LATTICE_BINARY
-// +, -, lattice.h:289-334; operator*(Lattice, double), lattice.h:348-356;
+// +, -, lattice.h:289-327,337-338; operator*(Lattice, double), lattice.h:348-356;
 // add_mul, lattice.h:358-364): a new field of the operands' shape, or in place
 template <class L>
 concept MeshField = std::is_base_of_v<BasicField<typename L::value_type>, L>;

@@ -144,7 +144,7 @@ int mesh_site_mul(mesh_field dst, mesh_field a, mesh_field b);
  * stack size); y may be NULL (out = a x), out may be x or y. Every field kind
  * stores its objects linearly (matrices, quaternions, complex numbers, packed
  * algebra), so this is the reference's lattice +, -, scalar * and their
- * compound forms (MESH_DEFINE_LATTICE_BINARY, lattice.h:289-334;
+ * compound forms (MESH_DEFINE_LATTICE_BINARY, lattice.h:289-327,337-338;
  * operator*(Lattice, double), lattice.h:348-356) and add_mul (lattice.h:358-364) */
 int mesh_field_axpby(mesh_field out, double a, mesh_field x, double b, mesh_field y);
 /* dst = exp(a), a an algebra field, dst a group field
