@@ -63,6 +63,13 @@ def test_version_and_errors_without_gpu(libpath):
     assert rc == 1 and b"unknown scheme" in L.mesh_last_error()
     buf = (ctypes.c_double * 64)()
     assert L.mesh_make_deltas(b"2mn", 0.5, 4, buf, 64, ctypes.byref(n)) == 0 and n.value == 17
+    # null handles are argument errors, checked before any device work
+    d = ctypes.c_double()
+    assert L.mesh_field_axpby(None, 1.0, None, 0.0, None) != 0
+    assert L.mesh_site_exp(None, None) != 0 and b"null" in L.mesh_last_error()
+    assert L.mesh_site_project(None, None) != 0
+    assert L.mesh_landau_line_search(None, None, None, 1.0, ctypes.byref(d)) != 0
+    assert L.mesh_landau_fa_set_accept(None, 1) != 0
 
 
 def test_make_deltas_matches_oracle(oracle, libpath):
