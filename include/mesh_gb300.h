@@ -225,19 +225,19 @@ int mesh_reunitize(mesh_field U);
 
 /* ---- HMC building blocks (src/gauge/hmc.h, hmc.cpp) ---------------------- */
 /* U_mu <- exp(project_on_algebra(P_mu) * t) U_mu for all mu (evolve,
- * hmc.h:249-257) */
+ * hmc.h:26-36) */
 int mesh_evolve(mesh_field U, mesh_field P, double t);
 /* P_mu -= wilsonDeriv(U, mu, beta) * delta for all mu (the momentum step
- * of runHmd, hmc.h:276-278), fused: staples, product, projection and update
+ * of runHmd, hmc.h:54-58), fused: staples, product, projection and update
  * in one kernel */
 int mesh_momentum_step(mesh_field P, mesh_field U, double beta, double delta);
-/* runHmd (hmc.h:261-280): alternating position/momentum steps */
+/* runHmd (hmc.h:38-59): alternating position/momentum steps */
 int mesh_run_hmd(mesh_field U, mesh_field P, double beta, const double *deltas, int n);
 /* makeDeltas (hmc.cpp:7-51): scheme "2lf", "2mn" or "4mn"; writes at most
  * capacity values and the count to *n */
 int mesh_make_deltas(const char *scheme, double epsilon, int substeps, double *out, int capacity, int *n);
 
-/* ---- HMC chain: Hmc<G> (hmc.h:287-336, hmc.cpp:394-445) ------------------
+/* ---- HMC chain: Hmc<G> (hmc.h:66-115, hmc.cpp:56-106) ------------------
  * Owns U, P and the proposal U_new. Momenta and the Metropolis uniform come
  * from counter-based device streams keyed by `seed` and the trajectory
  * number; H_old/H_new, dH and the accept decision are computed on the device
@@ -255,7 +255,7 @@ int mesh_hmc_create(mesh_ctx ctx, int group, int precision, int nd, const int32_
 int mesh_hmc_destroy(mesh_hmc h);
 /* borrowed handles of the state: which = 0 -> U, 1 -> P */
 int mesh_hmc_field(mesh_hmc h, int which, mesh_field *out);
-/* randomizeGaugeField (hmc.cpp:397-400) and a cold start */
+/* randomizeGaugeField (hmc.cpp:58-62) and a cold start */
 int mesh_hmc_randomize(mesh_hmc h);
 int mesh_hmc_cold_start(mesh_hmc h);
 /* Checkpoint and resume: U, the trajectory counter and the seed in a
@@ -275,7 +275,7 @@ int mesh_hmc_momentum_step(mesh_hmc h, double beta, double delta);
  * the one fused kernel the trajectory uses (the links are written out of
  * place and the chain's buffers swapped); otherwise as two kernels. */
 int mesh_hmc_md_step(mesh_hmc h, double beta, double dp, double du);
-/* runHmcUpdate (hmc.cpp:413-445): one trajectory, synchronous, record out */
+/* runHmcUpdate (hmc.cpp:73-107): one trajectory, synchronous, record out */
 int mesh_hmc_update(mesh_hmc h, double beta, const double *deltas, int n, mesh_hmc_record *rec);
 /* One trajectory on caller-supplied momenta P0 (algebra field, copied, not
  * modified) and Metropolis uniform: the parity entry point. */
@@ -297,7 +297,7 @@ int mesh_hmc_run_host(mesh_hmc h, void *host_U, size_t bytes, double beta, const
 /* ---- batched replicas (no reference counterpart) --------------------------
  * Many independent 4D lattices of one group and precision, each with its own
  * extents, beta and seed, advanced together: every step of the trajectory
- * sequence of runHmcUpdate (hmc.cpp:413-445) is one persistent launch over
+ * sequence of runHmcUpdate (hmc.cpp:73-107) is one persistent launch over
  * all replicas. Replica r follows the trajectory of a single chain
  * (mesh_hmc_*) created with seeds[r]: same momentum and Metropolis streams,
  * same per-link arithmetic. */

@@ -513,7 +513,7 @@ def gauge_transform(U: Field, g: Field) -> Field:
 
 # ---- HMC --------------------------------------------------------------------
 class Hmc:
-    """Hmc<G> (hmc.h:287-336): U, P, proposal, histories; momenta and the
+    """Hmc<G> (hmc.h:66-115): U, P, proposal, histories; momenta and the
     Metropolis uniform from counter-based device streams keyed by `seed`."""
 
     def __init__(self, ctx: Context, group, prec: int, grid: Grid, seed: int):

@@ -1,6 +1,6 @@
 // Batched replicas: many independent 4D lattices of one group and precision,
 // each with its own extents, beta and seed, advanced together by the HMC
-// trajectory sequence of runHmcUpdate (src/gauge/hmc.cpp:413-445) in which
+// trajectory sequence of runHmcUpdate (src/gauge/hmc.cpp:73-107) in which
 // every step is ONE persistent launch over all replicas.
 //
 // Layout in HBM: one allocation per field kind (U, U_new, P) holding the
@@ -549,7 +549,7 @@ struct mesh_batch_s
 		drop_graph();
 	}
 
-	// one trajectory of every replica (runHmcUpdate, hmc.cpp:413-445)
+	// one trajectory of every replica (runHmcUpdate, hmc.cpp:73-107)
 	void enqueue(double const *deltas, int n)
 	{
 		cudaStream_t st = ctx->stream;

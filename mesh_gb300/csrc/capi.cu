@@ -306,7 +306,7 @@ struct mesh_hmc_s
 		drop_graph();
 	}
 
-	// Enqueue one trajectory (runHmcUpdate, hmc.cpp:413-445) on the stream.
+	// Enqueue one trajectory (runHmcUpdate, hmc.cpp:73-107) on the stream.
 	// P0 != nullptr: supplied momenta; uniform NaN: draw from the stream.
 	void enqueue(double beta, double const *deltas, int n, Field const *P0, double uniform)
 	{
@@ -1117,7 +1117,7 @@ int mesh_hmc_update_supplied(mesh_hmc h, mesh_field P0, double uniform, double b
 		check_deltas(deltas, n);
 		DeviceGuard dg(h->ctx->device);
 		h->ensure_history(h->count + 1);
-		h->S_valid = false; // H_old from wilsonAction(U) as in hmc.cpp:423
+		h->S_valid = false; // H_old from wilsonAction(U) as in hmc.cpp:85
 		int64_t k = h->count;
 		h->enqueue(beta, deltas, n, &p0, uniform);
 		h->check_bad();

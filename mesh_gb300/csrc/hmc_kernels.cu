@@ -1,6 +1,6 @@
 // Device-side end of an HMC trajectory: the Metropolis test in FP64 on the
 // device (the reference draws the uniform and decides on the host,
-// src/gauge/hmc.cpp:423-431) and the accept-conditional copy of the proposal.
+// src/gauge/hmc.cpp:92-99) and the accept-conditional copy of the proposal.
 #include "field.cuh"
 #include "rng.cuh"
 

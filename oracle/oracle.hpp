@@ -8,7 +8,7 @@
 // slowest, one array-of-structs buffer per direction mu; src/lattice/grid.h:39-49,
 // src/lattice/lattice.h:159-192) and its algorithms op for op:
 //   group element math ........ src/gauge/groups.h:33-268
-//   cshift ..................... src/lattice/lattice.h:366-389, device.h:476-501
+//   cshift ..................... src/lattice/lattice.h:366-389, device.h:55-110
 //   reductions ................. src/lattice/device.h:185-212,246-265
 //                                (256-wide pairwise tree per block, serial
 //                                combine of the block partials, in the
@@ -863,14 +863,14 @@ inline std::vector<double> makeDeltas(std::string const &scheme, double epsilon,
 	return d;
 }
 
-// evolve (hmc.h:249-257): U = exp(project_on_algebra(P) * t) * U
+// evolve (hmc.h:26-36): U = exp(project_on_algebra(P) * t) * U
 template <class G> inline void evolve(Field<G> &U, Field<G> const &P, double t)
 {
 	using T = typename traits<G>::real;
 	site_loop(U.size(), [&](size_t i) { U[i] = gexp(project_on_algebra(P[i]) * T(t)) * U[i]; });
 }
 
-// runHmd (hmc.h:261-280)
+// runHmd (hmc.h:38-59)
 template <class G>
 inline void runHmd(Grid const &g, GaugeField<G> &U, GaugeField<G> &P, double beta,
                    std::vector<double> const &deltas)
@@ -900,7 +900,7 @@ struct HmcRecord
 	double plaq, dH, accept, H_old, H_new;
 };
 
-// runHmcUpdate (hmc.cpp:413-445) with the momenta and the Metropolis
+// runHmcUpdate (hmc.cpp:73-107) with the momenta and the Metropolis
 // uniform supplied by the caller instead of drawn from util::xoshiro256.
 template <class G>
 inline HmcRecord runHmcUpdate(Grid const &g, GaugeField<G> &U, GaugeField<G> const &P_in, double beta,

@@ -231,7 +231,7 @@ int ref_random_algebra_field(int grp, int prec, int nd, int const *dims, double 
 	});
 }
 
-// Hmc<G>::runHmcUpdate (hmc.cpp:413-445) with the momenta normals and the
+// Hmc<G>::runHmcUpdate (hmc.cpp:73-107) with the momenta normals and the
 // Metropolis uniform played back; rec = {plaquette, dH, accept}
 int ref_hmc_update(int grp, int prec, int nd, int const *dims, void *Up, double const *normals, size_t nn,
                    double uniform, double beta, double const *deltas, int n, double *rec)
