@@ -103,17 +103,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the fused MD-step kernel from the committed
-    ncu summary, scaled to the 32^4 launch (null when absent)."""
-    p = os.path.join(ROOT, "profiles", "md_step_su3_f32.md")
+def ncu_traffic(key="md_step_su3_f32_32^4"):
+    """DRAM bytes per launch of the dominant kernel from the data file of ncu
+    captures (profiles/dram_traffic.json); null when the file has no entry"""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
-        for line in open(p):
-            if line.startswith("dram_bytes_per_launch_32^4:"):
-                return float(line.split(":")[1].split()[0])
-    except OSError:
-        pass
-    return None
+        with open(p) as fh:
+            return float(json.load(fh)[key]["bytes_per_launch"])
+    except (OSError, KeyError, ValueError, TypeError):
+        return None
 
 
 class Clocks:

@@ -204,11 +204,16 @@ int mesh_wilson_loops(mesh_field U, int max_r, int max_t, double *out);
  * Its reduction scratch is a static device array inside the library of
  * MESH_NOALLOC_MAX_BLOCKS partial sums (8 KiB); a launch that would need more
  * blocks is refused with MESH_ERR_ARG (none does on devices of up to 256 SMs).
+ * `links` is checked with cudaPointerGetAttributes (no allocation): host
+ * memory or another device's buffer is refused with MESH_ERR_ARG before
+ * anything is launched.
  * The first call on a device does set-up (may create the device's primary
  * context and load the library's kernels, then resolves the scratch
- * address); make that call before any stream capture. Runs on `stream`
- * (NULL: the legacy default stream) and synchronises it. The scratch is
- * shared by all callers in the process: calls that overlap on one device
+ * address); make that call before any stream capture. A set-up that fails
+ * returns MESH_ERR_CUDA and is tried again by the next call. Every call
+ * runs on `stream` (NULL: the legacy default stream) and waits for it: the
+ * result is read back to the host before the function returns. The scratch
+ * is shared by all callers in the process: calls that overlap on one device
  * (several host threads, or work still in flight on another stream) race and
  * must be serialised by the caller. */
 #define MESH_NOALLOC_MAX_BLOCKS 1024

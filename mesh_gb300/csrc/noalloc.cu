@@ -33,9 +33,8 @@ constexpr int kMaxDevices = 64;
 
 struct NoAllocDevice
 {
-	std::once_flag once;
-	int status = MESH_ERR_CUDA;
-	char const *what = "set-up did not run";
+	std::mutex mu;
+	bool ready = false; // set only by a set-up that succeeded
 	double *scratch = nullptr;
 	int num_sms = 0;
 };
@@ -45,23 +44,49 @@ NoAllocDevice g_dev[kMaxDevices];
 // address and read the SM count. The first call on a device may also make
 // the CUDA runtime create the device's primary context and load this
 // module, which is the only device memory this path ever causes to exist.
-void setup(int device, NoAllocDevice &d)
+// A set-up that fails leaves the device not ready, so the next call tries
+// again (the cause, e.g. a device still busy being reset by its owner, may
+// have cleared); the failing call returns the error. Returns the failure's
+// message, or nullptr on success.
+char const *setup(int device, NoAllocDevice &d)
 {
+	std::lock_guard<std::mutex> lk(d.mu);
+	if (d.ready)
+		return nullptr;
+	double *p = nullptr;
 	int n = 0;
-	cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&d.scratch), g_noalloc_scratch);
+	if (cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return "cudaGetSymbolAddress of the no-allocation scratch failed";
+	}
+	if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0)
+	{
+		cudaGetLastError();
+		return "cudaDeviceGetAttribute(multiProcessorCount) failed";
+	}
+	d.scratch = p;
+	d.num_sms = n;
+	d.ready = true;
+	return nullptr;
+}
+
+// `links` must be device memory of `device` (or managed memory): a host
+// pointer or another device's buffer is refused here, before any launch.
+// cudaPointerGetAttributes allocates nothing.
+void check_links(int device, void const *links)
+{
+	cudaPointerAttributes a{};
+	cudaError_t e = cudaPointerGetAttributes(&a, links);
 	if (e != cudaSuccess)
 	{
-		d.what = "cudaGetSymbolAddress of the no-allocation scratch failed";
-		return;
+		cudaGetLastError();
+		throw Error(MESH_ERR_ARG, "links: not a pointer the CUDA runtime knows (device memory required)");
 	}
-	e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
-	if (e != cudaSuccess || n <= 0)
-	{
-		d.what = "cudaDeviceGetAttribute(multiProcessorCount) failed";
-		return;
-	}
-	d.num_sms = n;
-	d.status = MESH_OK;
+	if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+		throw Error(MESH_ERR_ARG, "links: host memory given where device memory of `device` is required");
+	if (a.device != device)
+		throw Error(MESH_ERR_ARG, "links: the buffer belongs to another device");
 }
 
 template <int GRP, class T, int ND>
@@ -107,8 +132,9 @@ extern "C" int mesh_plaquette_noalloc(int device, int group, int precision, int 
 		}
 		DeviceGuard dg(device);
 		NoAllocDevice &d = g_dev[device];
-		std::call_once(d.once, [&] { setup(device, d); });
-		require(d.status == MESH_OK, d.what, d.status);
+		if (char const *why = setup(device, d))
+			throw Error(MESH_ERR_CUDA, why);
+		check_links(device, links);
 		// the grid mesh_plaquette uses on this device (a function of the volume
 		// and the SM count only); a grid beyond the scratch is refused rather
 		// than shrunk, as a different grid would change the summation order

@@ -16,17 +16,21 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libref.so")
-REF_SRC = "/root/reference/src"
+# the reference's src/ directory, given by the environment (the build recipe
+# sets it where the reference tree is present); unset: nothing is built here
+REF_SRC = os.environ.get("MESH_REF_SRC", "")
 
 _lib = None
 
 
 def available() -> bool:
-    return os.path.exists(LIB_PATH) or os.path.isdir(REF_SRC)
+    return os.path.exists(LIB_PATH) or bool(REF_SRC and os.path.isdir(REF_SRC))
 
 
 def build():
-    out = subprocess.run(["make", "-C", HERE, "ref"], capture_output=True, text=True)
+    if not (REF_SRC and os.path.isdir(REF_SRC)):
+        raise RuntimeError("MESH_REF_SRC does not name the reference's src/ directory")
+    out = subprocess.run(["make", "-C", HERE, "ref", f"REF_SRC={REF_SRC}"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
 

@@ -19,6 +19,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
+# this script reads the reference checkout in place
+os.environ.setdefault("MESH_REF_SRC", "/root/reference/src")
 
 import pyref  # noqa: E402
 

@@ -72,6 +72,24 @@ def test_version_and_errors_without_gpu(libpath):
     assert L.mesh_landau_fa_set_accept(None, 1) != 0
 
 
+def test_noalloc_plaquette_refuses_without_launching(libpath):
+    """mesh_plaquette_noalloc given a host buffer (here, without a GPU, any
+    buffer): an error status and a message, no crash; argument errors come
+    before any CUDA call"""
+    import mesh_gb300 as mg
+
+    L = mg.load()
+    host = np.ones(4 * 256 * 18, dtype=np.float32)
+    d = (ctypes.c_int32 * 4)(4, 4, 4, 4)
+    out = ctypes.c_double(-1.0)
+    p = host.ctypes.data_as(ctypes.c_void_p)
+    assert L.mesh_plaquette_noalloc(0, 3, 1, 4, d, p, None, ctypes.byref(out)) != 0
+    assert L.mesh_last_error() and out.value == -1.0
+    bad = (ctypes.c_int32 * 4)(4, 4, 4, 5)
+    assert L.mesh_plaquette_noalloc(0, 3, 1, 4, bad, p, None, ctypes.byref(out)) == 1
+    assert b"even" in L.mesh_last_error()
+
+
 def test_make_deltas_matches_oracle(oracle, libpath):
     import mesh_gb300 as mg
     import numpy as np

@@ -50,6 +50,12 @@ def test_noalloc_plaquette_argument_errors(ctx):
     assert noalloc(L, 3, mg.F32, [4, 4, 4, 4], None)[0] == MESH_ERR_ARG
     d = (C.c_int32 * 4)(4, 4, 4, 4)
     assert L.mesh_plaquette_noalloc(-1, 3, mg.F32, 4, d, links, None, None) == MESH_ERR_ARG
+    # a host buffer where device memory is required: refused before any launch
+    import numpy as np
+
+    host = np.ones(4 * 256 * 18, dtype=np.float32)
+    assert noalloc(L, 3, mg.F32, [4, 4, 4, 4], host.ctypes.data_as(C.c_void_p))[0] == MESH_ERR_ARG
+    assert b"host memory" in L.mesh_last_error() or b"not a pointer" in L.mesh_last_error()
     # a valid call after the refused ones
     rc, got = noalloc(L, 3, mg.F32, [4, 4, 4, 4], links)
     assert rc == MESH_OK and got == 1.0
