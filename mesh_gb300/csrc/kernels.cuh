@@ -1360,6 +1360,10 @@ __global__ void __launch_bounds__(kBlock) k_gauge_transform(Geom g, T *__restric
 	}
 }
 
+} // namespace meshgb
+#include "md_line.cuh"
+namespace meshgb {
+
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
@@ -1587,8 +1591,10 @@ template <int GRP, class T, int ND> struct Ops
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
 	// packed FP32x2 products; 14-17, 21-28: thread per site
 	// (k_momentum_step_site) with FP32x2 products, tiles and launch shapes;
-	// 18-20: thread per site, plain products (every group and precision)
-	static constexpr int kForceVariants = 29;
+	// 18-20: thread per site, plain products (every group and precision);
+	// 29-32: SU(3) line march (k_md_line: plaquettes computed once, lower
+	// staples along x1 and x3 handed over), launch shapes and products
+	static constexpr int kForceVariants = 33;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1621,7 +1627,11 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/f32x2", 1},
 		    {2, {2, 1, 1, 3}, 128, 4, "site/tile4x2x2x8/128thr/4blk/f32x2", 1},
 		    {2, {0, 0, 3, 4}, 128, 4, "site/tile1x1x8x16/128thr/4blk/f32x2", 1},
-		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1}};
+		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk"},
+		    {3, {0, 0, 0, 0}, 256, 2, "line/256thr/2blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2", 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1633,6 +1643,8 @@ template <int GRP, class T, int ND> struct Ops
 			return false;
 		if (!fv.tiled)
 			return true;
+		if (fv.tiled == 3)
+			return GRP == SU3 && ND == 4 && line_supported(g);
 		if (ND != 4)
 			return false;
 		for (int i = 0; i < 4; ++i)
@@ -1668,6 +1680,12 @@ template <int GRP, class T, int ND> struct Ops
 		else if constexpr (ND == 4)
 		{
 			unsigned b = 0;
+			if (fv.tiled == 3)
+			{
+				launch_line<ROWS, false>(fv, g, u, p, coef, kin, c, nullptr, T(0), 0);
+				MESH_LAUNCH_CHECK();
+				return;
+			}
 			TileSpec ts = tiles_for(g, fv, c, b);
 			if (fv.tiled == 2)
 				launch_force_site<ROWS>(fv, b, g, ts, u, p, coef, kin, c);
@@ -1729,6 +1747,48 @@ template <int GRP, class T, int ND> struct Ops
 			k_momentum_step_site<GRP, T, 4, 256, 2, F2, ROWS, FUSE>
 			    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 	}
+	// the line-march kernel (SU(3), four dimensions): persistent grid of at
+	// most minb blocks per SM, every warp one contiguous range of line steps
+	template <bool ROWS, bool FUSE>
+	static void launch_line(ForceVariant const &fv, Geom const &g, T const *u, T *p, T coef, RedSlot kin,
+	                        Context &c, T *uo, T tu, int reunit)
+	{
+		if constexpr (GRP == SU3 && ND == 4)
+		{
+			LineSpec ls{};
+			ls.ns = 32 / g.L[3];
+			ls.ncol = g.L[0] * (g.L[2] / ls.ns);
+			ls.items = int64_t(ls.ncol) * g.L[1];
+			// FP64 slots take twice the shared memory: 64-thread blocks
+			int threads = sizeof(T) == 8 ? 64 : fv.threads;
+			int minb = sizeof(T) == 8 ? 6 : fv.minb;
+			int wpb = threads / 32;
+			int64_t need = (ls.items + wpb - 1) / wpb;
+			int64_t cap = int64_t(c.num_sms) * minb;
+			unsigned b = unsigned(need < cap ? need : cap);
+			ls.nwarps = int64_t(b) * wpb;
+			if constexpr (sizeof(T) == 8)
+				k_md_line<T, 64, 6, 0, ROWS, FUSE><<<b, 64, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+			else
+			{
+				if (fv.f2)
+					line_cfg<1, ROWS, FUSE>(fv, b, g, ls, u, p, coef, kin, c, uo, tu, reunit);
+				else
+					line_cfg<0, ROWS, FUSE>(fv, b, g, ls, u, p, coef, kin, c, uo, tu, reunit);
+			}
+		}
+	}
+	template <int F2, bool ROWS, bool FUSE>
+	static void line_cfg(ForceVariant const &fv, unsigned b, Geom const &g, LineSpec const &ls, T const *u, T *p,
+	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
+	{
+		if (fv.threads == 256)
+			k_md_line<T, 256, 2, F2, ROWS, FUSE><<<b, 256, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+		else if (fv.minb == 3)
+			k_md_line<T, 128, 3, F2, ROWS, FUSE><<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+		else
+			k_md_line<T, 128, 4, F2, ROWS, FUSE><<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+	}
 	// tiles of variant fv over g and the grid size (at most minb blocks per SM)
 	static TileSpec tiles_for(Geom const &g, ForceVariant const &fv, Context const &c, unsigned &b)
 	{
@@ -1747,7 +1807,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 28; // the thread-per-site variants
+	static constexpr int kMdFirst = 14, kMdLast = 32; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
@@ -1770,10 +1830,16 @@ template <int GRP, class T, int ND> struct Ops
 			Geom const &g = Uin.geom;
 			ForceVariant fv = force_variant(v);
 			unsigned b = 0;
-			TileSpec ts = tiles_for(g, fv, c, b);
 			T const *u = static_cast<T const *>(Uin.d);
 			T *p = static_cast<T *>(P.d);
 			T *uo = static_cast<T *>(Uout.d);
+			if (fv.tiled == 3)
+			{
+				launch_line<R, true>(fv, g, u, p, coef, kin, c, uo, tu, reunit);
+				MESH_LAUNCH_CHECK();
+				return;
+			}
+			TileSpec ts = tiles_for(g, fv, c, b);
 			if constexpr (kF2)
 			{
 				if (fv.f2)

@@ -1,0 +1,482 @@
+// Momentum step (optionally fused with the link update after it) for SU(3) in
+// four dimensions, organised by lattice lines: one warp holds the L3 sites
+// x3 = 0..L3-1 of 32/L3 neighbouring lines (fixed x0, x1, x2), and marches
+// along x1. The operation is the reference's momentum step of runHmd
+// (src/gauge/hmc.h:54-58: P_mu -= wilsonDeriv(U, mu, beta) dt, with
+// wilsonDeriv = project_on_algebra(U_mu stapleSum_mu) beta/(2 Nc),
+// src/gauge/utils.h:114-153), followed, when fused, by evolve
+// (src/gauge/hmc.h:26-36).
+//
+// The force on link (x, mu) is the sum over the six plaquettes that contain
+// it of the projection of the loop that starts with that link. A plaquette
+// P = U_mu(x) U_nu(x+mu) U_mu(x+nu)^+ U_nu(x)^+ (mu < nu), A = proj(P),
+// contributes
+//     +A                      to (x, mu)      (its upper staple),
+//     -A                      to (x, nu),
+//     -U_nu(x)^+ A U_nu(x)    to (x+nu, mu)   (the lower staple of that link),
+//     +U_mu(x)^+ A U_mu(x)    to (x+mu, nu),
+// because proj(V^+ M V) = V^+ proj(M) V for unitary V and the lower-staple
+// loop of (x+nu, mu) is U_nu(x)^+ P^+ U_nu(x). Each site computes its six
+// plaquettes once (3 products each, from rows 0 and 1 where the links are
+// special unitary) and hands the lower-staple contributions along the two
+// directions the warp can reach cheaply as 8-real algebra elements:
+//   * along x3 to the next lane of the same warp, through shared memory;
+//   * along x1 to the next line of the march, carried by the same thread.
+// The lower staples along x0 and x2 are summed as in the reference
+// (U_nu(y+mu)^+ U_mu(y)^+ U_nu(y) at y = x - nu, one product U_mu(x) S_mu
+// for the sum). Against computing every staple per link this saves six of
+// the twelve lower-staple products of a site and most neighbour loads: a
+// site reads its own four links, the twelve forward neighbours
+// U_nu(x + mu) and the links of the x0 and x2 lower staples.
+//
+// Work assignment: "columns" of lines (x0, x2-group) times x1 form a list of
+// L0 (L2 ns / 32...) line steps in column-major order; every warp of the
+// persistent grid takes one contiguous range of it, so all warps hold the
+// same number of steps to within one. At the first step of a range, and when
+// a range passes into the next column, the carry along x1 is computed for the
+// line behind (three plaquettes and their contributions).
+//
+// The sum runs in a different order than the reference's staple sum, which
+// changes the force only at the rounding level.
+//
+// Included by kernels.cuh after the thread-per-site kernels, whose helpers
+// (LinkLoad, Prod, add_plane, plane_mu/nu, comp, grid_sum) it uses.
+#pragma once
+
+namespace meshgb {
+
+struct LineSpec
+{
+	int ns;         // lines per warp = 32 / L3
+	int ncol;       // columns = L0 * L2 / ns
+	int64_t items;  // line steps = ncol * L1
+	int64_t nwarps; // warps of the launch
+};
+
+inline bool line_supported(Geom const &g)
+{
+	if (g.nd != 4)
+		return false;
+	int l3 = g.L[3];
+	if (l3 < 2 || l3 > 32 || 32 % l3 != 0)
+		return false;
+	int ns = 32 / l3;
+	return g.L[2] % ns == 0;
+}
+
+template <class T, int F2> struct LineProd
+{
+	using Gp = Group<SU3, T>;
+	using E = typename Gp::E;
+	// rows 0, 1 of a b (rows 0, 1 of a read)
+	__device__ __forceinline__ static E mul01(E const &a, E const &b)
+	{
+		if constexpr (F2)
+			return Su3F2::template mul<2>(a, b);
+		else
+		{
+			E r;
+#pragma unroll
+			for (int i = 0; i < 2; ++i)
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+				{
+					T re = 0, im = 0;
+#pragma unroll
+					for (int k = 0; k < 3; ++k)
+					{
+						re += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * j] - a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * j + 1];
+						im += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * j + 1] + a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * j];
+					}
+					r.v[6 * i + 2 * j] = re;
+					r.v[6 * i + 2 * j + 1] = im;
+				}
+			return r;
+		}
+	}
+	// rows 0, 1 of a b^+ (rows 0, 1 of a and all of b read)
+	__device__ __forceinline__ static E mul01_nd(E const &a, E const &b)
+	{
+		if constexpr (F2)
+			return Su3F2::template prod<2>(
+			    [&](int i, int k, float &re, float &im) {
+				    re = a.v[6 * i + 2 * k];
+				    im = a.v[6 * i + 2 * k + 1];
+			    },
+			    [&](int k, int j, float &re, float &im) {
+				    re = b.v[6 * j + 2 * k];
+				    im = -b.v[6 * j + 2 * k + 1];
+			    });
+		else
+		{
+			E r;
+#pragma unroll
+			for (int i = 0; i < 2; ++i)
+#pragma unroll
+				for (int j = 0; j < 3; ++j)
+				{
+					T re = 0, im = 0;
+#pragma unroll
+					for (int k = 0; k < 3; ++k)
+					{
+						T ar = a.v[6 * i + 2 * k], ai = a.v[6 * i + 2 * k + 1];
+						T br = b.v[6 * j + 2 * k], bi = b.v[6 * j + 2 * k + 1];
+						re += ar * br + ai * bi;
+						im += ai * br - ar * bi;
+					}
+					r.v[6 * i + 2 * j] = re;
+					r.v[6 * i + 2 * j + 1] = im;
+				}
+			return r;
+		}
+	}
+	// proj (antihermitian traceless part, packed) of a special unitary matrix
+	// given by rows 0 and 1: the row-2 entries it needs come from
+	// row 2 = conj(row 0 x row 1)
+	__device__ __forceinline__ static void proj01(E const &p, T *o)
+	{
+		cx<T> p20 = cconj(csub(cmul(p.at(0, 1), p.at(1, 2)), cmul(p.at(0, 2), p.at(1, 1))));
+		cx<T> p21 = cconj(csub(cmul(p.at(0, 2), p.at(1, 0)), cmul(p.at(0, 0), p.at(1, 2))));
+		// Im conj(p00 p11 - p01 p10)
+		T i22 = -((p.v[0] * p.v[9] + p.v[1] * p.v[8]) - (p.v[2] * p.v[7] + p.v[3] * p.v[6]));
+		T t = (p.v[1] + p.v[9] + i22) * T(1.0 / 3.0);
+		o[0] = p.v[1] - t;
+		o[1] = p.v[9] - t;
+		o[2] = (p.v[2] - p.v[6]) * T(0.5);
+		o[3] = (p.v[3] + p.v[7]) * T(0.5);
+		o[4] = (p.v[4] - p20.re) * T(0.5);
+		o[5] = (p.v[5] + p20.im) * T(0.5);
+		o[6] = (p.v[10] - p21.re) * T(0.5);
+		o[7] = (p.v[11] + p21.im) * T(0.5);
+	}
+	// sg V^+ A V for A = from_alg(o) and unitary V, packed (upper triangle
+	// and the imaginary diagonal of the exactly antihermitian traceless
+	// result)
+	__device__ __forceinline__ static void adjoint(E const &V, T const *o, T sg, T *out)
+	{
+		// B = A V with A_ii = i a_i, A_ij = -conj(A_ji)
+		T a0 = o[0], a1 = o[1], a2 = -(o[0] + o[1]);
+		cx<T> A01 = {o[2], o[3]}, A02 = {o[4], o[5]}, A12 = {o[6], o[7]};
+		cx<T> A10 = {-o[2], o[3]}, A20 = {-o[4], o[5]}, A21 = {-o[6], o[7]};
+		cx<T> B[3][3];
+#pragma unroll
+		for (int j = 0; j < 3; ++j)
+		{
+			cx<T> v0 = V.at(0, j), v1 = V.at(1, j), v2 = V.at(2, j);
+			B[0][j] = cadd(cx<T>{-a0 * v0.im, a0 * v0.re}, cadd(cmul(A01, v1), cmul(A02, v2)));
+			B[1][j] = cadd(cx<T>{-a1 * v1.im, a1 * v1.re}, cadd(cmul(A10, v0), cmul(A12, v2)));
+			B[2][j] = cadd(cx<T>{-a2 * v2.im, a2 * v2.re}, cadd(cmul(A20, v0), cmul(A21, v1)));
+		}
+		// C = V^+ B: C_ij = sum_k conj(V_ki) B_kj
+		auto cij = [&](int i, int j) {
+			cx<T> z = {T(0), T(0)};
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				z = cadd(z, cmul(cconj(V.at(k, i)), B[k][j]));
+			return z;
+		};
+		auto cii_im = [&](int i) {
+			T z = T(0);
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				cx<T> v = V.at(k, i);
+				z += v.re * B[k][i].im - v.im * B[k][i].re;
+			}
+			return z;
+		};
+		cx<T> c01 = cij(0, 1), c02 = cij(0, 2), c12 = cij(1, 2);
+		out[0] = sg * cii_im(0);
+		out[1] = sg * cii_im(1);
+		out[2] = sg * c01.re;
+		out[3] = sg * c01.im;
+		out[4] = sg * c02.re;
+		out[5] = sg * c02.im;
+		out[6] = sg * c12.re;
+		out[7] = sg * c12.im;
+	}
+};
+
+// site coordinates of the line march (x3 of the lane, x2 of its sub-line)
+struct LineSite
+{
+	int x0, x1, x2, x3;
+};
+
+__device__ __forceinline__ int wrap_add(int x, int d, int L)
+{
+	x += d;
+	return x >= L ? x - L : (x < 0 ? x + L : x);
+}
+
+// even/odd index of the site (a0, a1, a2, a3) (coordinates in range)
+__device__ __forceinline__ int64_t line_eo(Geom const &g, int a0, int a1, int a2, int a3)
+{
+	int32_t lex = ((a0 * g.L[1] + a1) * g.L[2] + a2) * g.L[3] + a3;
+	int p = (a0 + a1 + a2 + a3) & 1;
+	return int64_t(p) * g.Vh + (lex >> 1);
+}
+
+// site x shifted by s1 along d1 and s2 along d2 (s = 0: no shift)
+__device__ __forceinline__ int64_t line_nb(Geom const &g, LineSite const &x, int d1, int s1, int d2 = 0, int s2 = 0)
+{
+	int c[4] = {x.x0, x.x1, x.x2, x.x3};
+#pragma unroll
+	for (int i = 0; i < 4; ++i)
+	{
+		int d = (i == d1 ? s1 : 0) + (i == d2 ? s2 : 0);
+		c[i] = wrap_add(c[i], d, g.L[i]);
+	}
+	return line_eo(g, c[0], c[1], c[2], c[3]);
+}
+
+// A = proj of the plaquette (mu, nu) at site x (mu < nu, runtime)
+template <class T, int F2, class LD>
+__device__ __forceinline__ void line_plaquette(Geom const &g, LineSite const &x, int64_t s, int mu, int nu,
+                                               LD const &ld, T *o)
+{
+	using Pr = LineProd<T, F2>;
+	using Gp = Group<SU3, T>;
+	using E = typename Gp::E;
+	E M1 = Pr::mul01(ld.rows(mu, s), ld(nu, line_nb(g, x, mu, +1)));
+	E M2 = Pr::mul01(ld.rows(nu, s), ld(mu, line_nb(g, x, nu, +1)));
+	Gp::complete_row2(M2);
+	Pr::proj01(Pr::mul01_nd(M1, M2), o);
+}
+
+// the three planes that send along x1: (0,1) to link 0 with -U_1^+ A U_1,
+// (1,2) to link 2 and (1,3) to link 3 with +U_1^+ A U_1; along x3: (0,3),
+// (1,3), (2,3) to links 0, 1, 2 with -U_3^+ A U_3
+__device__ __forceinline__ int plane_q(int mu, int nu) { return mu == 0 ? nu - 1 : (mu == 1 ? nu + 1 : 5); }
+
+// shared-memory hand-over slots of one warp: 8 reals per (link k, lane) as
+// 16-byte words, [k][word][lane], so that a warp's access is contiguous
+template <class T> struct Slot16;
+template <> struct Slot16<float>
+{
+	using W = float4;
+	static constexpr int N = 2; // words per algebra element
+	__device__ __forceinline__ static W pack(float const *o) { return W{o[0], o[1], o[2], o[3]}; }
+	__device__ __forceinline__ static void unpack(W w, float *o)
+	{
+		o[0] = w.x;
+		o[1] = w.y;
+		o[2] = w.z;
+		o[3] = w.w;
+	}
+};
+template <> struct Slot16<double>
+{
+	using W = double2;
+	static constexpr int N = 4;
+	__device__ __forceinline__ static W pack(double const *o) { return W{o[0], o[1]}; }
+	__device__ __forceinline__ static void unpack(W w, double *o)
+	{
+		o[0] = w.x;
+		o[1] = w.y;
+	}
+};
+
+template <class T> __device__ __forceinline__ void slot_store(typename Slot16<T>::W *sl, int k, int lane, T const *o)
+{
+	using S = Slot16<T>;
+#pragma unroll
+	for (int w = 0; w < S::N; ++w)
+		sl[(S::N * k + w) * 32 + lane] = S::pack(o + w * (8 / S::N));
+}
+template <class T>
+__device__ __forceinline__ void slot_load(typename Slot16<T>::W const *sl, int k, int lane, T *o)
+{
+	using S = Slot16<T>;
+#pragma unroll
+	for (int w = 0; w < S::N; ++w)
+		S::unpack(sl[(S::N * k + w) * 32 + lane], o + w * (8 / S::N));
+}
+
+// F[mu] += x for a runtime mu (selects keep F in registers)
+template <int NA, class T> __device__ __forceinline__ void add_link(T (&F)[4][NA], int mu, T const *x, T sg = T(1))
+{
+#pragma unroll
+	for (int k = 0; k < 4; ++k)
+		if (k == mu)
+		{
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				F[k][a] += sg * x[a];
+		}
+}
+
+// carry of the line behind x (x - e_1): the contributions of its planes
+// (0,1), (1,2), (1,3) to links 0, 2, 3 of x, into the carry slots
+template <class T, int F2, class LD>
+__device__ __forceinline__ void line_carry(Geom const &g, LineSite const &x, LD const &ld,
+                                           typename Slot16<T>::W *carry, int lane)
+{
+	using Pr = LineProd<T, F2>;
+	using Gp = Group<SU3, T>;
+	using E = typename Gp::E;
+	LineSite y = x;
+	y.x1 = wrap_add(x.x1, -1, g.L[1]);
+	int64_t sy = line_eo(g, y.x0, y.x1, y.x2, y.x3);
+#pragma unroll 1
+	for (int k = 0; k < 3; ++k)
+	{
+		int mu = k == 0 ? 0 : 1, nu = k == 0 ? 1 : k + 1;
+		T o[8], c[8];
+		line_plaquette<T, F2>(g, y, sy, mu, nu, ld, o);
+		E V = ld(1, sy);
+		Pr::adjoint(V, o, k == 0 ? T(-1) : T(1), c);
+		slot_store<T>(carry, k, lane, c);
+	}
+}
+
+// One momentum step (and with FUSE the link update after it) of every link,
+// line-marching. P -= coef F(U); Uout = exp(tu P) U (reunitised when reunit).
+template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE>
+__global__ void __launch_bounds__(NT, MINB)
+    k_md_line(Geom g, LineSpec ls, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
+              T *__restrict__ Uout, T tu, int reunit)
+{
+	using Gp = Group<SU3, T>;
+	using E = typename Gp::E;
+	using Pr = LineProd<T, F2>;
+	using PrO = Prod<SU3, T, F2>;
+	using SW = typename Slot16<T>::W;
+	constexpr int NA = 8;
+	constexpr int NW = NT / 32;
+	constexpr int NS = 3 * Slot16<T>::N * 32;
+	// per warp: hand-over along x3 (3 links) and the carry along x1 (3 links)
+	__shared__ SW sm_x3[NW][NS];
+	__shared__ SW sm_x1[NW][NS];
+	LinkLoad<SU3, T, 4, ROWS> ld{U, g.V};
+	int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+	SW *s3 = sm_x3[wib];
+	SW *s1 = sm_x1[wib];
+	int64_t wid = int64_t(blockIdx.x) * NW + wib;
+	int64_t i0 = wid * ls.items / ls.nwarps, i1 = (wid + 1) * ls.items / ls.nwarps;
+	int L1 = g.L[1], L3 = g.L[3];
+	int sub = lane / L3;
+	int lane_prev = sub * L3 + (lane % L3 == 0 ? L3 - 1 : lane % L3 - 1);
+	int ngrp = g.L[2] / ls.ns;
+	double acc = 0.0;
+	for (int64_t it = i0; it < i1; ++it)
+	{
+		int col = int(it / L1);
+		LineSite x;
+		x.x1 = int(it - int64_t(col) * L1);
+		x.x0 = col / ngrp;
+		x.x2 = (col - x.x0 * ngrp) * ls.ns + sub;
+		x.x3 = lane % L3;
+		int64_t s = line_eo(g, x.x0, x.x1, x.x2, x.x3);
+		if (it == i0 || x.x1 == 0)
+			line_carry<T, F2>(g, x, ld, s1, lane);
+		T F[4][NA];
+		// the carry from x - e_1: links 0, 2, 3
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			F[1][a] = T(0);
+		slot_load<T>(s1, 0, lane, F[0]);
+		slot_load<T>(s1, 1, lane, F[2]);
+		slot_load<T>(s1, 2, lane, F[3]);
+		__syncwarp();
+		// the six plaquettes of x
+#pragma unroll 1
+		for (int q = 0; q < 6; ++q)
+		{
+			int mu = plane_mu<4>(q), nu = plane_nu<4>(q);
+			T o[8];
+			line_plaquette<T, F2>(g, x, s, mu, nu, ld, o);
+			add_plane<4, NA>(F, q, o);
+			// hand-overs: along x1 (planes with mu or nu = 1), along x3 (nu = 3)
+#pragma unroll 1
+			for (int r = 0; r < 2; ++r)
+			{
+				int dir = r == 0 ? 1 : 3;
+				bool send = r == 0 ? (mu == 1 || nu == 1) : (nu == 3);
+				if (!send)
+					continue;
+				// the receiving link and the sign: (mu, nu) with dir == nu goes
+				// to link mu with -V^+ A V, dir == mu to link nu with +
+				int k = dir == nu ? mu : nu;
+				T sg = dir == nu ? T(-1) : T(1);
+				T c[8];
+				Pr::adjoint(ld(dir, s), o, sg, c);
+				if (r == 0)
+					slot_store<T>(s1, k == 0 ? 0 : k - 1, lane, c);
+				else
+					slot_store<T>(s3, k, lane, c);
+			}
+		}
+		// lower staples along x0 and x2, summed per link and closed with U_mu(x)
+#pragma unroll 1
+		for (int mu = 0; mu < 4; ++mu)
+		{
+			E S = Gp::zero();
+#pragma unroll 1
+			for (int r = 0; r < 2; ++r)
+			{
+				int nu = r == 0 ? 0 : 2;
+				if (nu == mu)
+					continue;
+				int64_t y = line_nb(g, x, nu, -1);
+				E f = ld(nu, line_nb(g, x, nu, -1, mu, +1));
+				E ef = PrO::mul_r2(ld.rows(mu, y), f);
+				Gp::add_to(S, PrO::mul_dn(ef, ld(nu, y)));
+			}
+			E W = PrO::mul(ld(mu, s), S);
+			T xa[NA];
+			Gp::proj(W, xa);
+			add_link<NA>(F, mu, xa);
+		}
+		// contributions from x - e_3 (the previous lane): links 0, 1, 2
+		__syncwarp();
+		{
+			T c[8];
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				slot_load<T>(s3, k, lane_prev, c);
+				add_link<NA>(F, k, c);
+			}
+		}
+		__syncwarp();
+		// momentum update and (FUSE) the link update
+#pragma unroll 1
+		for (int mu = 0; mu < 4; ++mu)
+		{
+			T f[NA];
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+			{
+				f[a] = F[0][a];
+#pragma unroll
+				for (int k = 1; k < 4; ++k)
+					f[a] = mu == k ? F[k][a] : f[a];
+			}
+			auto Pv = comp<T, NA>(P, g.V, mu);
+			T p[NA];
+			Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				p[a] -= coef * f[a];
+			Pv.template store<CACHE_STREAM>(s, p);
+			if (kin.result)
+				acc += double(Gp::kin(p));
+			if constexpr (FUSE)
+			{
+				E r;
+				if constexpr (ROWS)
+					r = PrO::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
+				else
+					r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
+				if (reunit)
+					r = Gp::reunit_fast(r);
+				comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
+			}
+		}
+	}
+	if (kin.result)
+		grid_sum<NT>(acc, kin);
+}
+
+} // namespace meshgb
