@@ -6,7 +6,11 @@
 //   lattice_apply(f, a, as...)       f(T&, Ts const&...) on every site
 //   lattice_sum_apply(f, a, as...)   sum over sites of f(T const&, Ts const&...)
 //   lattice_sum(a)                   sum of the objects
-//   cshift(dst, src, dir, offset)    dst[x] = src[x + offset e_dir]
+//   cshift(nd, dims, dst, src, dir, offset)   dst[x] = src[x + offset e_dir]
+// a, as... are FieldView<T> (device base pointer and V). The forms above run
+// on the legacy default stream; lattice_apply_on / lattice_sum_apply_on take
+// the stream first. Functors are __device__ lambdas (nvcc --extended-lambda)
+// or structs with a __device__ operator().
 //
 // Storage. A field of V objects of type T (trivially copyable, sizeof(T) a
 // multiple of 4) is held even/odd-ordered as structure-of-arrays "planes" of
@@ -127,10 +131,14 @@ __global__ void apply_kernel(F f, int64_t V, FieldView<T> a, FieldView<Ts>... as
 
 // lattice_apply (lattice.h:256-261, device.h:219-228)
 template <class F, class T, class... Ts>
-void lattice_apply(F f, int64_t V, FieldView<T> a, FieldView<Ts>... as, cudaStream_t stream = nullptr)
+void lattice_apply_on(cudaStream_t stream, F f, FieldView<T> a, FieldView<Ts>... as)
 {
-	apply_kernel<<<grid_blocks(V), 256, 0, stream>>>(f, V, a, as...);
+	apply_kernel<<<grid_blocks(a.V), 256, 0, stream>>>(f, a.V, a, as...);
 	cuda_ok(cudaGetLastError(), "lattice_apply launch");
+}
+template <class F, class T, class... Ts> void lattice_apply(F f, FieldView<T> a, FieldView<Ts>... as)
+{
+	lattice_apply_on(cudaStream_t(nullptr), f, a, as...);
 }
 
 template <int BLOCK, class R, class F, class T, class... Ts>
@@ -159,9 +167,17 @@ __global__ void sum_kernel(F f, int64_t V, R *partials, unsigned *counter, R *re
 	__syncthreads();
 	if (last && threadIdx.x == 0)
 	{
+		// the other blocks' partials, read past L1 (written by other SMs)
 		R r{};
 		for (unsigned b = 0; b < gridDim.x; ++b)
-			r += static_cast<R volatile *>(partials)[b];
+		{
+			R v;
+			unsigned char volatile const *src = reinterpret_cast<unsigned char volatile const *>(partials + b);
+			unsigned char *dst = reinterpret_cast<unsigned char *>(&v);
+			for (size_t k = 0; k < sizeof(R); ++k)
+				dst[k] = src[k];
+			r += v;
+		}
 		*result = r;
 	}
 }
@@ -169,11 +185,12 @@ __global__ void sum_kernel(F f, int64_t V, R *partials, unsigned *counter, R *re
 // lattice_sum_apply (lattice.h:263-268, device.h:185-212,246-265); returns
 // the sum on the host (synchronises the stream, as the reference does)
 template <class F, class T, class... Ts>
-auto lattice_sum_apply(F f, int64_t V, FieldView<T> a, FieldView<Ts>... as, cudaStream_t stream = nullptr)
+auto lattice_sum_apply_on(cudaStream_t stream, F f, FieldView<T> a, FieldView<Ts>... as)
 {
 	using R = std::decay_t<decltype(f(std::declval<T const &>(), std::declval<Ts const &>()...))>;
 	static_assert(std::is_trivially_copyable_v<R>, "sum type must be trivially copyable");
 	constexpr int B = 256;
+	int64_t V = a.V;
 	unsigned blocks = grid_blocks(V, B);
 	if (blocks > 1024)
 		blocks = 1024;
@@ -192,11 +209,21 @@ auto lattice_sum_apply(F f, int64_t V, FieldView<T> a, FieldView<Ts>... as, cuda
 	cuda_ok(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
 	return host;
 }
+template <class F, class T, class... Ts> auto lattice_sum_apply(F f, FieldView<T> a, FieldView<Ts>... as)
+{
+	return lattice_sum_apply_on(cudaStream_t(nullptr), f, a, as...);
+}
+
+// the functor of lattice_sum: the object itself
+struct Identity
+{
+	template <class T> __device__ T operator()(T const &x) const { return x; }
+};
 
 // lattice_sum (lattice.h:270-273)
-template <class T> T lattice_sum(int64_t V, FieldView<T> a, cudaStream_t stream = nullptr)
+template <class T> T lattice_sum(FieldView<T> a, cudaStream_t stream = nullptr)
 {
-	return lattice_sum_apply([] __device__(T const &x) { return x; }, V, a, stream);
+	return lattice_sum_apply_on(stream, Identity{}, a);
 }
 
 // geometry for cshift on the even/odd order (all extents even)

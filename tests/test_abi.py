@@ -219,3 +219,23 @@ def test_cpp_wilson_loops_instantiate(libpath, tmp_path):
     r = subprocess.run(["g++", "-std=c++20", "-O1", "-Wall", "-Werror", "-c", "-I", os.path.join(ROOT, "include"),
                         str(src), "-o", str(tmp_path / "w.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_functor_layer_compiles_with_user_functors(tmp_path):
+    """include/mesh/lattice_apply.cuh compiles for sm_103a with the user
+    functors of the GPU test (a __device__ lambda, functor structs, a struct
+    sum type, cshift); no GPU needed to compile"""
+    import shutil
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    import test_gpu_functor_layer as t
+
+    src = tmp_path / "user_functors.cu"
+    src.write_text(t.SRC)
+    r = subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-std=c++20", "--extended-lambda",
+                        "-c", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(tmp_path / "u.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
