@@ -480,6 +480,23 @@ int oracle_landau_deriv(int grp, int prec, int nd, int const *dims, void const *
 	});
 }
 
+// line_search (landau.h:77-98) from the transform gt along F
+int oracle_landau_line_search(int grp, int prec, int nd, int const *dims, void const *U, void const *gt,
+                              void const *F, double eps, double *out)
+{
+	return guarded([&] {
+		Grid g(nd, dims);
+		dispatch(grp, prec, [&](auto tag) {
+			using G = decltype(tag);
+			auto u = load_stack<G>(g, nd, U);
+			Landau<G> l(g, u);
+			l.g = load_field<G>(g, gt);
+			int n = 0;
+			*out = l.line_search(load_field<G>(g, F), eps, &n);
+		});
+	});
+}
+
 // reference CG + line search (landau.h:100-136), threshold as a parameter
 int oracle_landau_cg(int grp, int prec, int nd, int const *dims, void const *U, void *gt, int max_iter,
                      double tol, int *iters, double *theta, int *n_evals)

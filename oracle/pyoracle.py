@@ -79,6 +79,7 @@ def lib():
             "oracle_landau_condition": (I, [I, I, I, IP, P, P, DP]),
             "oracle_landau_deriv": (I, [I, I, I, IP, P, P, P]),
             "oracle_landau_cg": (I, [I, I, I, IP, P, P, I, D, IP, DP, IP]),
+            "oracle_landau_line_search": (I, [I, I, I, IP, P, P, P, D, DP]),
             "oracle_landau_or_sweeps": (I, [I, I, I, IP, P, P, D, I]),
             "oracle_landau_or": (I, [I, I, I, IP, P, P, D, D, I, I, IP, DP]),
             "oracle_landau_theta": (I, [I, I, I, IP, P, P, DP, DP]),
@@ -372,6 +373,15 @@ def landau_deriv(group, prec, dims, U, g):
     _chk(lib().oracle_landau_deriv(group, prec, nd, d, _ptr(np.ascontiguousarray(U)),
                                    _ptr(np.ascontiguousarray(g)), _ptr(F)))
     return F
+
+
+def landau_line_search(group, prec, dims, U, g, F, eps):
+    nd, d = _dims(dims)
+    out = C.c_double()
+    _chk(lib().oracle_landau_line_search(group, prec, nd, d, _ptr(np.ascontiguousarray(U)),
+                                         _ptr(np.ascontiguousarray(g)), _ptr(np.ascontiguousarray(F)), eps,
+                                         C.byref(out)))
+    return out.value
 
 
 def landau_cg(group, prec, dims, U, g, max_iter, tol):

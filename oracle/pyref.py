@@ -57,6 +57,9 @@ def lib():
             "ref_cshift": (I, [I, I, I, IP, P, I, I, P]),
             "ref_random_algebra_field": (I, [I, I, I, IP, DP, C.c_size_t, P]),
             "ref_hmc_update": (I, [I, I, I, IP, P, DP, C.c_size_t, D, D, DP, I, DP]),
+            "ref_landau_eval": (I, [I, I, I, IP, P, P, DP, DP, P]),
+            "ref_landau_line_search": (I, [I, I, I, IP, P, P, P, D, DP]),
+            "ref_landau_run": (I, [I, I, I, IP, P, P, I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -175,3 +178,30 @@ def hmc_update(grp, prec, dims, U, normals, uniform, beta, deltas):
     _chk(lib().ref_hmc_update(grp, prec, nd, d, _p(U), _dp(nrm), nrm.size, uniform, beta, _dp(dl), len(dl),
                               _dp(rec)))
     return U, dict(plaq=rec[0], dH=rec[1], accept=rec[2])
+
+
+def landau_eval(group, prec, dims, U, g):
+    """the reference's Landau<G> on (U, g): (functional, condition, deriv)"""
+    nd, d = _dims(dims)
+    f, c = C.c_double(), C.c_double()
+    g = np.ascontiguousarray(g)
+    F = np.zeros_like(g)
+    _chk(lib().ref_landau_eval(group, prec, nd, d, _p(np.ascontiguousarray(U)), _p(g), C.byref(f), C.byref(c), _p(F)))
+    return f.value, c.value, F
+
+
+def landau_line_search(group, prec, dims, U, g, F, eps):
+    nd, d = _dims(dims)
+    out = C.c_double()
+    g = np.ascontiguousarray(g)
+    _chk(lib().ref_landau_line_search(group, prec, nd, d, _p(np.ascontiguousarray(U)), _p(g), _p(np.ascontiguousarray(F)), eps, C.byref(out)))
+    return out.value
+
+
+def landau_run(group, prec, dims, U, g, max_iter):
+    """the reference's Landau<G>::run(max_iter) from g; returns the new g"""
+    nd, d = _dims(dims)
+    g = np.ascontiguousarray(g.copy())
+    _chk(lib().ref_landau_run(group, prec, nd, d, _p(np.ascontiguousarray(U)), _p(g), max_iter))
+    return g
+

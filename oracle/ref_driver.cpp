@@ -2,15 +2,42 @@
 //
 // Drives the reference's own templates, compiled in place from the reference
 // tree (src/lattice/grid.h, lattice.h, tensor.h; src/gauge/groups.h, utils.h,
-// hmc.h, hmc.cpp) against the project-written stand-ins in oracle/ref_shim.
+// hmc.h, hmc.cpp, landau.h) against the project-written stand-ins in
+// oracle/ref_shim.
 // Built by `make -C oracle ref` into oracle/_ref/libref.so (x86 or Arm, never
 // committed); only the tests that pin the restated oracle load it.
 #include "gauge/hmc.h"
+#include "gauge/landau.h"
 
 #include <exception>
 #include <string>
 
 using namespace mesh;
+
+// Landau<G>::reset() is the one line of src/gauge/landau.h (:14, g.fill(G(1)))
+// that does not compile as shipped: Lattice::fill is commented out in
+// src/lattice/lattice.h:59. It is replaced here, for the six instantiations
+// used, by an explicit specialisation that sets g to the unit element through
+// copy_from_host; the primary definition is then never instantiated and every
+// other member of Landau<G> (landau.h:23-136) is the reference's own.
+namespace {
+template <class T> util::complex<T> unit_of(util::complex<T> *) { return {T(1), T(0)}; }
+template <class T> util::quaternion<T> unit_of(util::quaternion<T> *) { return {T(1), T(0), T(0), T(0)}; }
+template <class T, int N> util::Matrix<T, N> unit_of(util::Matrix<T, N> *) { return util::Matrix<T, N>::identity(); }
+template <class G> void set_unit(Lattice<G> &g)
+{
+	std::vector<G> h(g.grid().size(), unit_of(static_cast<G *>(nullptr)));
+	g.copy_from_host(std::span<const G>(h.data(), h.size()));
+}
+} // namespace
+namespace mesh {
+template <> void Landau<U1<float>>::reset() { set_unit(g); }
+template <> void Landau<U1<double>>::reset() { set_unit(g); }
+template <> void Landau<SU2<float>>::reset() { set_unit(g); }
+template <> void Landau<SU2<double>>::reset() { set_unit(g); }
+template <> void Landau<SU3<float>>::reset() { set_unit(g); }
+template <> void Landau<SU3<double>>::reset() { set_unit(g); }
+} // namespace mesh
 
 namespace {
 thread_local std::string g_err;
@@ -36,6 +63,11 @@ template <class G> void store1(Lattice<G> const &L, void *p)
 {
 	auto h = L.copy_to_host();
 	std::memcpy(p, (void const *)h.data(), h.size() * sizeof(G));
+}
+
+template <class G> void load1(Lattice<G> &L, void const *p)
+{
+	L.copy_from_host(std::span<const G>(static_cast<G const *>(p), L.grid().size()));
 }
 
 template <class F> int guarded(F f)
@@ -254,4 +286,58 @@ int ref_hmc_update(int grp, int prec, int nd, int const *dims, void *Up, double 
 		});
 	});
 }
+
+// ---- Landau<G> (src/gauge/landau.h) on supplied links U and transform g ----
+// operator() (landau.h:23-34), condition() (:37-49), deriv() (:52-65)
+int ref_landau_eval(int grp, int prec, int nd, int const *dims, void const *Up, void const *gp, double *functional,
+                    double *condition, void *deriv)
+{
+	return guarded([&] {
+		auto gr = make_grid(nd, dims);
+		dispatch(grp, prec, [&]<class G>() {
+			GaugeField<G> U(gr);
+			load(U, nd, gr.size(), Up);
+			Landau<G> L(U);
+			load1(L.g, gp);
+			*functional = L();
+			*condition = L.condition();
+			store1(L.deriv(), deriv);
+		});
+	});
 }
+
+// line_search(F, eps) (landau.h:77-98) from the transform g
+int ref_landau_line_search(int grp, int prec, int nd, int const *dims, void const *Up, void const *gp,
+                           void const *Fp, double eps, double *out)
+{
+	return guarded([&] {
+		auto gr = make_grid(nd, dims);
+		dispatch(grp, prec, [&]<class G>() {
+			GaugeField<G> U(gr);
+			load(U, nd, gr.size(), Up);
+			Landau<G> L(U);
+			load1(L.g, gp);
+			Lattice<G> F(gr);
+			load1(F, Fp);
+			*out = L.line_search(F, eps);
+		});
+	});
+}
+
+// run(max_iter) (landau.h:100-136) from the transform g (g updated in place)
+int ref_landau_run(int grp, int prec, int nd, int const *dims, void const *Up, void *gp, int max_iter)
+{
+	return guarded([&] {
+		auto gr = make_grid(nd, dims);
+		dispatch(grp, prec, [&]<class G>() {
+			GaugeField<G> U(gr);
+			load(U, nd, gr.size(), Up);
+			Landau<G> L(U);
+			load1(L.g, gp);
+			L.run(max_iter);
+			store1(L.g, gp);
+		});
+	});
+}
+}
+

@@ -84,6 +84,17 @@ def main():
             Uh, rec = pyref.hmc_update(grp, 2, dims, U, normals, 0.25, beta, d2lf)
             out["hmc_U"] = Uh
             out["hmc_rec"] = np.array([rec["plaq"], rec["dH"], rec["accept"]])
+        # Landau<G> (landau.h:23-136, reset() replaced by a unit fill): the
+        # functional, condition and deriv at a Haar-random transform g, the
+        # line search along that deriv from the reference's starting step,
+        # and g after 25 iterations of run() (the Polak-Ribiere steps start
+        # after iteration 20)
+        g = haar(grp, V, rng).astype(np.float64)
+        out["landau_g"] = g
+        f, c, F = pyref.landau_eval(grp, 2, dims, U, g)
+        out["landau_functional"], out["landau_condition"], out["landau_deriv"] = f, c, F
+        out["landau_line_search"] = pyref.landau_line_search(grp, 2, dims, U, g, F, 3000.0)
+        out["landau_run25_g"] = pyref.landau_run(grp, 2, dims, U, g, 25)
         np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
         print(name, "plaquette", out["plaquette"])
 

@@ -53,6 +53,32 @@ def test_oracle_matches_reference_golden(oracle, path):
         assert [r["plaq"], r["dH"], r["accept"]] == list(z["hmc_rec"])
 
 
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_landau_matches_reference_golden(oracle, path):
+    """The Landau restatement against the reference's own Landau<G>
+    (landau.h:23-136; its reset(), whose g.fill does not compile as shipped,
+    replaced by a unit fill): functional, deriv, the line search along that
+    deriv and g after 25 CG iterations bit for bit in FP64. The condition
+    agrees bit for bit for U(1) and SU(3); for SU(2) the oracle's (and the
+    library's) theta uses the 2x2-matrix norm 2|q|^2 of the algebra element,
+    twice the quaternion norm |q|^2 of the util stand-in the reference build
+    is compiled against (the same norm choice that keeps the SU(2)
+    Hamiltonian consistent)."""
+    z = np.load(path)
+    g, dims = int(z["group"]), [int(x) for x in z["dims"]]
+    U, gt = z["U"], z["landau_g"]
+    assert oracle.landau_functional(g, 2, dims, U, gt) == z["landau_functional"]
+    cond = oracle.landau_condition(g, 2, dims, U, gt)
+    assert cond == (2 * z["landau_condition"] if g == 2 else z["landau_condition"])
+    F = oracle.landau_deriv(g, 2, dims, U, gt)
+    np.testing.assert_array_equal(F, z["landau_deriv"])
+    assert oracle.landau_line_search(g, 2, dims, U, gt, F, 3000.0) == z["landau_line_search"]
+    # run() stops at condition < 1e-10 (landau.h:113); 25 iterations stay above it
+    g25, iters, _, _ = oracle.landau_cg(g, 2, dims, U, gt, 25, 1e-10)
+    assert iters == 25
+    np.testing.assert_array_equal(g25, z["landau_run25_g"])
+
+
 def test_oracle_matches_reference_live(oracle):
     """Same comparison against a fresh in-place build of the reference, on
     other inputs and in FP32 too (skipped where the reference tree is absent)."""

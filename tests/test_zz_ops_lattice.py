@@ -88,11 +88,17 @@ def test_landau_line_search_is_the_cg_step(ctx, oracle, g):
     and s = line_search(F, 3000)"""
     dims = [4, 4, 4, 8]
     grid = mg.Grid(dims)
-    U = gauge(ctx, g, 2, dims, thermal(oracle, g, dims))
+    U64 = thermal(oracle, g, dims)
+    U = gauge(ctx, g, 2, dims, U64)
     L = mg.Landau(U)
     F = L.deriv()
     s = L.line_search(F, 3000.0)
     assert s > 0
+    # the step itself against the oracle's line search (pinned to the
+    # reference's Landau<G>::line_search by the golden fixtures)
+    g1 = oracle.unit_transform(g, 2, dims)
+    s_o = oracle.landau_line_search(g, 2, dims, U64, g1, oracle.landau_deriv(g, 2, dims, U64, g1), 3000.0)
+    assert s == pytest.approx(s_o, rel=1e-10)
     X = mg.axpby(mg.Lattice(ctx, g, 2, grid, algebra=True), s, F)
     h = mg.site_mul(mg.Lattice(ctx, g, 2, grid), mg.site_exp(mg.Lattice(ctx, g, 2, grid), X), L.g)
     mg.reunitize(h)
