@@ -35,6 +35,8 @@ WORKLOAD = dict(name="su3_hmc_32^4_beta6.0_2mn_eps0.5_n20_mixed", group=3, dims=
                 scheme="2mn", eps=0.5, substeps=20, seed=7, therm=200)
 METRIC = "SU(3) 32^4 HMC trajectories/s"
 UNIT = "traj/s"
+# timed CPU work of the reference arm (complete trajectories, at least one)
+REF_TIME_LIMIT = 120.0
 
 
 def parse():
@@ -46,8 +48,15 @@ def parse():
     ap.add_argument("--therm", type=int, default=WORKLOAD["therm"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-physics", action="store_true",
+                    help="skip the FP64-vs-mixed-precision chains of the headline line")
+    ap.add_argument("--physics-traj", type=int, default=100,
+                    help="trajectories of each chain of the FP64-vs-mixed comparison")
+    ap.add_argument("--no-landau", action="store_true", help="skip the one-configuration Landau number")
     ap.add_argument("--lattice", type=int, default=32,
                     help="extent L of the L^4 lattice (32 = the headline workload; smaller for profiling captures)")
+    ap.add_argument("--dims", type=int, nargs=4, default=None,
+                    help="the four extents of a non-hypercubic lattice for profiling captures (overrides --lattice)")
     ap.add_argument("--workload", choices=["hmc", "batch", "landau", "wilson", "heatbath", "fp64-8x4"], default="hmc",
                     help="hmc: the headline line; batch: 64 SU(2) replicas in one persistent launch against 64 "
                          "separate chains; landau: time to theta < 1e-12, overrelaxation vs Fourier-accelerated "
@@ -62,7 +71,10 @@ def parse():
                     help="hmc workload: the plain all-FP64 chain (links, momenta, force in FP64) instead of the "
                          "mixed-precision one, for the FP64-vs-mixed comparison")
     a = ap.parse_args()
-    if a.lattice != 32:
+    if a.dims:
+        WORKLOAD["dims"] = list(a.dims)
+        WORKLOAD["name"] = WORKLOAD["name"].replace("32^4", "x".join(map(str, a.dims)))
+    elif a.lattice != 32:
         WORKLOAD["dims"] = [a.lattice] * 4
         WORKLOAD["name"] = WORKLOAD["name"].replace("32^4", f"{a.lattice}^4")
     if a.fp64:
@@ -103,9 +115,30 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(key="md_step_su3_f32_32^4"):
+KERNEL_DESC = {
+    "line": "k_md_line<float,...,rows01,fused> (SU(3) line march: six plaquettes per site computed once, lower "
+            "staples along x1 and x3 handed over, along x0 and x2 summed per link; momentum update and the "
+            "following link update in the same pass)",
+    "site": "k_momentum_step_site<SU3,float,4,..,rows01,fused> (staples + force + momentum update + the following "
+            "link update, one thread per site; links read as rows 0,1, row 2 rebuilt)",
+    "separate": "momentum step and link update as two kernels",
+}
+
+
+def chosen_variant(report, prefix):
+    """the launch variant the autotuner chose for the first key starting with
+    `prefix` (e.g. 'line/128thr/4blk/f32x2'), or 'separate'"""
+    for ln in report.splitlines():
+        if ln.startswith(prefix) and "chosen " in ln:
+            c = ln.split("chosen ", 1)[1].split(" [", 1)[0]
+            return "separate" if c.startswith("separate") else c
+    return "unknown"
+
+
+def ncu_traffic(key):
     """DRAM bytes per launch of the dominant kernel from the data file of ncu
-    captures (profiles/dram_traffic.json); null when the file has no entry"""
+    captures (profiles/dram_traffic.json, keyed by the launch variant of the
+    32^4 workload); null when the file has no entry"""
     p = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(p) as fh:
@@ -163,21 +196,101 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline_md(U_host, P_host, dims, n, beta, delta, threads=0):
-    """The reference algorithm (oracle restatement) on the host cores: one
-    momentum step + one link update + one plaquette on the full lattice,
-    extrapolated to a trajectory of n_P momentum and n_U link steps plus two
-    actions, a momentum refresh and a reunitisation (each costed as a link
-    update)."""
+def cpu_trajectories(U_host, dims, deltas, beta, seed, count=1, time_limit=None, threads=0):
+    """Complete trajectories of the reference algorithm (the oracle's C++
+    restatement of runHmcUpdate, FP32, OpenMP on the host cores) on the full
+    lattice: momentum refresh, H_old, the MD steps of `deltas`, reunitisation,
+    H_new and the Metropolis test, timed one by one. Runs `count`
+    trajectories, or stops early once `time_limit` seconds are spent (at
+    least one). Returns (seconds per trajectory list, cores)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build()
     cores = pyoracle.set_threads(threads)
-    tf, te, tp = pyoracle.bench_md(WORKLOAD["group"], 1, dims, U_host, P_host, beta, delta, 1)
-    n_u, n_p = deltas_counts(n)
-    t_traj = n_p * tf + (n_u + 2) * te + 2 * tp
-    return 1.0 / t_traj, cores, tf, te, tp
+    U = U_host
+    times = []
+    for k in range(count):
+        t0 = time.perf_counter()
+        U, _ = pyoracle.hmc_chain(WORKLOAD["group"], 1, dims, U, beta, deltas, seed, k, 1)
+        times.append(time.perf_counter() - t0)
+        if time_limit is not None and sum(times) >= time_limit:
+            break
+    return times, cores
+
+
+def chain_stats(hist, bin_size=10):
+    """plaquette mean with the standard error from bins of `bin_size`
+    trajectories, acceptance, <exp(-dH)> with its binned error, mean dH"""
+    import numpy as np
+
+    def binned(x):
+        x = np.asarray(x, dtype=np.float64)
+        nb = len(x) // bin_size
+        if nb < 2:
+            return float(x.mean()), float("nan")
+        b = x[:nb * bin_size].reshape(nb, bin_size).mean(axis=1)
+        return float(x.mean()), float(b.std(ddof=1) / np.sqrt(nb))
+
+    p, pe = binned(hist["plaq_history"])
+    e, ee = binned(np.exp(-np.asarray(hist["deltaH_history"])))
+    return {"trajectories": int(len(hist["plaq_history"])), "plaquette": p, "plaquette_err": pe,
+            "acceptance": float(np.mean(hist["accept_history"])), "exp_minus_dH": e, "exp_minus_dH_err": ee,
+            "dH_mean": float(np.mean(hist["deltaH_history"]))}
+
+
+def physics_fp64_vs_mixed(ctx, U_host, grid, d, beta, ntraj):
+    """Two chains from the same thermalised links and the same seed (so the
+    same momentum and Metropolis streams): the mixed-precision one (FP32
+    links, momenta, force; FP64 sums, dH, Metropolis) and the all-FP64 one,
+    `ntraj` trajectories each. Errors from bins of 10 trajectories; the
+    plaquette difference is compared with the two errors combined as if the
+    chains were independent (they are correlated, so this is conservative)."""
+    import numpy as np
+
+    import mesh_gb300 as mg
+
+    res = {}
+    t = {}
+    for name, prec, arr in (("mixed", mg.F32, U_host), ("fp64", mg.F64, U_host.astype(np.float64))):
+        h = mg.Hmc(ctx, 3, prec, grid, seed=11)
+        h.U.import_(arr)
+        t0 = time.perf_counter()
+        h.run(beta, d, ntraj, use_graph=True)
+        h.history()
+        t[name] = time.perf_counter() - t0
+        res[name] = chain_stats(h.history())
+        res[name]["traj_per_s"] = ntraj / t[name]
+        h.close()
+    dp = res["mixed"]["plaquette"] - res["fp64"]["plaquette"]
+    err = float(np.hypot(res["mixed"]["plaquette_err"], res["fp64"]["plaquette_err"]))
+    res["plaquette_diff"] = dp
+    res["plaquette_diff_err"] = err
+    res["within_2_sigma"] = bool(abs(dp) < 2 * err)
+    res["run"] = (f"{ntraj} trajectories per chain from the headline chain's thermalised links, seed 11, "
+                  f"2mn eps={WORKLOAD['eps']} n={WORKLOAD['substeps']}, beta={beta}")
+    return res
+
+
+def landau_one_config(ctx, L=24, therm=100):
+    """Landau gauge fixing of one thermalised SU(3) L^4 beta = 6.0
+    configuration (HMC seed 1, Haar-random transform seed 5) to
+    theta < 1e-12: FP64 overrelaxation (omega 1.7), Fourier acceleration with
+    the plain and with the learned multiplier (steps accepted on theta,
+    overrelaxation fallback): seconds, iterations, fallbacks, functional."""
+    from mesh_gb300 import landau_learn as ll
+
+    (beta, Uh), = list(ll.hmc_configs(ctx, L, [6.0], [1], therm, 1, 0))
+    params, _ = ll.load_weights()
+    out = {"lattice": [L] * 4, "thermalisation": f"{therm} trajectories, seed 1", "transform_seed": 5}
+    for method in ("or", "plain", "learned"):
+        U = ll.prepared_links(ctx, Uh, transform_seed=5)
+        r = ll.solve(ctx, U, method, params, beta)
+        out[method] = {k: r[k] for k in ("seconds", "iterations", "fallbacks", "theta", "functional")}
+        U.close()
+    for m in ("plain", "learned"):
+        out[f"speedup_{m}_vs_or"] = out["or"]["seconds"] / out[m]["seconds"]
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -200,6 +313,11 @@ def job_time_and_rate(ms, steps, world, dist=None, device="cpu"):
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores (the oracle restatement,
+    FP32 = the reference's precision=1 path, all host threads): every step
+    is one complete trajectory of the 32^4 workload. One untimed trajectory
+    first; the timed steps stop after REF_TIME_LIMIT seconds (at least one),
+    so that the run ends within a few minutes; `steps` reports how many ran."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -209,26 +327,25 @@ def run_reference(args):
     import pyoracle
 
     pyoracle.build()
-    dims, n = WORKLOAD["dims"], 0
+    dims = WORKLOAD["dims"]
     d = pyoracle.make_deltas(WORKLOAD["scheme"], WORKLOAD["eps"], WORKLOAD["substeps"])
-    n = len(d)
     U = pyoracle.random_gauge(3, 1, dims, WORKLOAD["seed"])
-    P = pyoracle.random_momenta(3, 1, dims, WORKLOAD["seed"], 0)
-    vals = []
-    for k in range(args.warmup + args.steps):
-        v, cores, tf, te, tp = cpu_baseline_md(U, P, dims, n, WORKLOAD["beta"], float(d[1]))
-        if k >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
-    sample = (f"per step: one momentum step ({tf:.2f} s), one link update ({te:.2f} s) and one plaquette "
-              f"({tp:.2f} s) of the reference algorithm on the full 32^4 SU(3) FP32 lattice, extrapolated to a "
-              f"{WORKLOAD['scheme']} n={WORKLOAD['substeps']} trajectory")
+    warm, cores = cpu_trajectories(U, dims, d, WORKLOAD["beta"], WORKLOAD["seed"], count=min(1, args.warmup))
+    times, cores = cpu_trajectories(U, dims, d, WORKLOAD["beta"], WORKLOAD["seed"] + 1, count=args.steps,
+                                    time_limit=REF_TIME_LIMIT)
+    value = len(times) / sum(times)
+    sample = (f"{len(times)} complete trajectories ({WORKLOAD['scheme']} n={WORKLOAD['substeps']}: momentum "
+              f"refresh, two actions, {len(d) // 2 + 1} link updates, {len(d) // 2} momentum steps, "
+              f"reunitisation, Metropolis) of the reference algorithm on the full 32^4 SU(3) FP32 lattice, "
+              f"{np.mean(times):.1f} s each, timed one by one after {len(warm)} untimed; capped at "
+              f"{REF_TIME_LIMIT:.0f} s of timed work")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+            "steps": len(times), "warmup": len(warm), "ms_per_step": 1000.0 / value, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD["name"], "lattice": dims, "beta": WORKLOAD["beta"],
                        "integrator": f"{WORKLOAD['scheme']} eps={WORKLOAD['eps']} n={WORKLOAD['substeps']}",
-                       "precision": "FP32 (the reference's precision=1 path)", "parallelism": "cpu threads"},
+                       "precision": "FP32 (the reference's precision=1 path)", "parallelism": "cpu threads",
+                       "steps_requested": args.steps, "warmup_requested": args.warmup},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -329,6 +446,7 @@ def run_ours(args):
     t_evolve = ev0.elapsed_time(ev1) / reps / 1000.0
     peak, peak_kind = measured_peaks()
     achieved = B_md / t_md / 1e9
+    md_variant = chosen_variant(mg.tune_report(), "md_step/")
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -343,12 +461,8 @@ def run_ours(args):
                       "timing": "CUDA events on the launching stream, CUDA-graph replay of whole trajectories"},
            "physics": {"acceptance": acc, "plaquette_mean": plaq, "exp_minus_dH_mean": edH},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": ncu_traffic(),
-                        "kernel": "k_momentum_step_site<SU3,float,4,..,f32x2,rows01,fused> (staples + force + "
-                                  "momentum update + the following link update, one thread per site; links read "
-                                  "as rows 0,1, row 2 rebuilt)" if pb == 4 else
-                                  "k_momentum_step_tiled<SU3,double> + k_evolve<SU3,double> (FP64: momentum step "
-                                  "and link update as two kernels)",
+                        "frac": achieved / peak, "traffic": ncu_traffic(f"md_step/{md_variant}"),
+                        "kernel": KERNEL_DESC.get(md_variant.split("/")[0], md_variant) + f" [{md_variant}]",
                         "algorithmic_bytes_per_launch": B_md, "avg_launch_ms": t_md * 1e3,
                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                         else "fallback 6.8 TB/s"},
@@ -382,13 +496,16 @@ def run_ours(args):
                       "api": "mesh_hmc_run_host (import U, one trajectory, export U)"}
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline and pb == 4:
-        Uh = U.export()
-        Ph = P.export()
-        v, cores, tf, te, tp = cpu_baseline_md(Uh, Ph, dims, n, beta, float(d[1]))
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": f"one momentum step ({tf:.2f} s), one link update ({te:.2f} s), one "
-                                         f"plaquette ({tp:.2f} s) of the reference algorithm (oracle/ C++ "
-                                         f"restatement, FP32) on the full 32^4 lattice, extrapolated to a trajectory"}
+        times, cores = cpu_trajectories(U.export(), dims, list(d), beta, WORKLOAD["seed"] + 100, count=1)
+        out["cpu_baseline"] = {"value": 1.0 / times[0], "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"one complete trajectory ({times[0]:.1f} s: momentum refresh, two "
+                                         f"actions, {n_u} link updates, {n_p} momentum steps, reunitisation, "
+                                         f"Metropolis) of the reference algorithm (oracle/ C++ restatement, "
+                                         f"FP32) on the full 32^4 lattice from this run's thermalised links"}
+    if rank == 0 and world == 1 and not args.no_physics and pb == 4:
+        out["physics_fp64_vs_mixed"] = physics_fp64_vs_mixed(ctx, U.export(), grid, d, beta, args.physics_traj)
+    if rank == 0 and world == 1 and not args.no_landau and pb == 4:
+        out["landau_24x4"] = landau_one_config(ctx)
     if rank == 0:
         print(json.dumps(out), flush=True)
     h.close()

@@ -1586,15 +1586,17 @@ template <int GRP, class T, int ND> struct Ops
 		int threads, minb;
 		char const *name;
 		int f2 = 0;        // packed FP32x2 products (SU(3) float only)
+		int r2 = 0;        // line march: row 2 of whole-link loads read, not rebuilt
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
 	// packed FP32x2 products; 14-17, 21-28: thread per site
 	// (k_momentum_step_site) with FP32x2 products, tiles and launch shapes;
 	// 18-20: thread per site, plain products (every group and precision);
-	// 29-32: SU(3) line march (k_md_line: plaquettes computed once, lower
-	// staples along x1 and x3 handed over), launch shapes and products
-	static constexpr int kForceVariants = 33;
+	// 29-34: SU(3) line march (k_md_line: plaquettes computed once, lower
+	// staples along x1 and x3 handed over), launch shapes, products and
+	// whether row 2 of whole links is read or rebuilt
+	static constexpr int kForceVariants = 35;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1631,7 +1633,9 @@ template <int GRP, class T, int ND> struct Ops
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2", 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk"},
 		    {3, {0, 0, 0, 0}, 256, 2, "line/256thr/2blk/f32x2", 1},
-		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2", 1}};
+		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2", 1, 1},
+		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2/row2", 1, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1782,6 +1786,19 @@ template <int GRP, class T, int ND> struct Ops
 	static void line_cfg(ForceVariant const &fv, unsigned b, Geom const &g, LineSpec const &ls, T const *u, T *p,
 	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
 	{
+		if constexpr (ROWS && F2)
+		{
+			if (fv.r2)
+			{
+				if (fv.minb == 3)
+					k_md_line<T, 128, 3, F2, ROWS, FUSE, true>
+					    <<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+				else
+					k_md_line<T, 128, 4, F2, ROWS, FUSE, true>
+					    <<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+				return;
+			}
+		}
 		if (fv.threads == 256)
 			k_md_line<T, 256, 2, F2, ROWS, FUSE><<<b, 256, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
 		else if (fv.minb == 3)
@@ -1807,7 +1824,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 32; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 34; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)

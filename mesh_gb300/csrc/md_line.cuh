@@ -197,6 +197,42 @@ template <class T, int F2> struct LineProd
 	}
 };
 
+// link loads of the line march: rows() reads rows 0 and 1 (the left factor
+// of a product of special unitary links); operator() reads the whole link,
+// with row 2 rebuilt from rows 0, 1 (R2 = false: 48 bytes read, 24 FMAs) or
+// read from memory (R2 = true: 72 bytes, no arithmetic). FP64 links and
+// ROWS = false read every real.
+template <class T, bool ROWS, bool R2> struct LineLoad
+{
+	using Gp = Group<SU3, T>;
+	using E = typename Gp::E;
+	T const *U;
+	int64_t V;
+	__device__ __forceinline__ E operator()(int mu, int64_t s) const
+	{
+		E e;
+		if constexpr (ROWS && !R2)
+		{
+			Soa<T, 18>::template load_head<12, CACHE_KEEP>(U + int64_t(mu) * 18 * V, V, s, e.v);
+			Gp::complete_row2(e);
+		}
+		else
+			Soa<T, 18>::template load<CACHE_KEEP>(U + int64_t(mu) * 18 * V, V, s, e.v);
+		return e;
+	}
+	__device__ __forceinline__ E rows(int mu, int64_t s) const
+	{
+		if constexpr (ROWS)
+		{
+			E e;
+			Soa<T, 18>::template load_head<12, CACHE_KEEP>(U + int64_t(mu) * 18 * V, V, s, e.v);
+			return e;
+		}
+		else
+			return (*this)(mu, s);
+	}
+};
+
 // site coordinates of the line march (x3 of the lane, x2 of its sub-line)
 struct LineSite
 {
@@ -332,7 +368,7 @@ __device__ __forceinline__ void line_carry(Geom const &g, LineSite const &x, LD 
 
 // One momentum step (and with FUSE the link update after it) of every link,
 // line-marching. P -= coef F(U); Uout = exp(tu P) U (reunitised when reunit).
-template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE>
+template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE, bool R2 = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_md_line(Geom g, LineSpec ls, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
               T *__restrict__ Uout, T tu, int reunit)
@@ -348,7 +384,7 @@ __global__ void __launch_bounds__(NT, MINB)
 	// per warp: hand-over along x3 (3 links) and the carry along x1 (3 links)
 	__shared__ SW sm_x3[NW][NS];
 	__shared__ SW sm_x1[NW][NS];
-	LinkLoad<SU3, T, 4, ROWS> ld{U, g.V};
+	LineLoad<T, ROWS, R2> ld{U, g.V};
 	int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	SW *s3 = sm_x3[wib];
 	SW *s1 = sm_x1[wib];

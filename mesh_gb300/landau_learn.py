@@ -110,15 +110,17 @@ def family_table(alpha, high, p2min, p2max, n=TABLE_N, low=1.0):
     return np.log(family_mult(alpha, high, p2, p2min, p2max, low)).astype(np.float32), lo, hi
 
 
-def survey(ctx, L, seeds, members, therm=100, transform_seed=5, max_iter=5000):
+def survey(ctx, L, seeds, members, therm=100, transform_seed=5, max_iter=5000, accept="theta"):
     """Fixed multipliers family_mult(alpha, high, low) over configurations:
     {member: [(steps, fallbacks, cost), ...]} with cost = steps + 11 x
-    fallbacks; a member that does not converge in max_iter steps costs 99999."""
+    fallbacks; a member that does not converge in max_iter steps costs 99999.
+    Steps are accepted on `accept` ("theta" or "functional")."""
     res = {m: [] for m in members}
     for beta, Uh in hmc_configs(ctx, L, [6.0] * len(seeds), seeds, therm, 1, 0):
         for m in members:
             U = prepared_links(ctx, Uh, transform_seed)
             fa = LandauFA(U)
+            fa.set_accept(accept == "functional")
             p2min, p2max = fa.p2range()
             fa.set_table(*family_table(m[0], m[1], p2min, p2max, low=m[2]))
             g = Lattice(ctx, 3, F64, U.grid).set_unit()
@@ -128,7 +130,8 @@ def survey(ctx, L, seeds, members, therm=100, transform_seed=5, max_iter=5000):
     return res
 
 
-def collect(ctx, U, beta, tol=1e-12, nbins=24, max_steps=400, omega=1.7, or_sweeps=10, sample=None):
+def collect(ctx, U, beta, tol=1e-12, nbins=24, max_steps=400, omega=1.7, or_sweeps=10, sample=None,
+            accept="theta", alphas=None, highs=None):
     """Samples along a data-collection run, one set per decade of theta. At
     the start of a decade every member (alpha, high) of the multiplier
     family runs on a copy of g under the solver's own policy (a step that
@@ -139,9 +142,14 @@ def collect(ctx, U, beta, tol=1e-12, nbins=24, max_steps=400, omega=1.7, or_swee
     target for the features (log p^2/p2max, beta, theta) at the decade's
     start and middle; g advances to that member's result. With `sample` (a
     set of decade numbers, 0 = the first) only those decades are searched;
-    the others advance with the plain multiplier. Rows: (3 features,
+    the others advance with the plain multiplier. Steps are accepted on
+    `accept` ("theta" or "functional"; under the functional test no step
+    falls back and the cost is the number of steps). Rows: (3 features,
     target)."""
+    alphas = ALPHAS if alphas is None else alphas
+    highs = HIGHS if highs is None else highs
     fa = LandauFA(U)
+    fa.set_accept(accept == "functional")
     p2min, p2max = fa.p2range()
     g = Lattice(U.ctx, 3, F64, U.grid).set_unit()
     trial = Lattice(U.ctx, 3, F64, U.grid)
@@ -166,8 +174,8 @@ def collect(ctx, U, beta, tol=1e-12, nbins=24, max_steps=400, omega=1.7, or_swee
             continue
         best = None
         plain_cost = None
-        for a in ALPHAS:
-            for b in HIGHS:
+        for a in alphas:
+            for b in highs:
                 fa.set_table(*family_table(a, b, p2min, p2max))
                 trial.copy_from(g)
                 it, fb, th_end = fa.run(trial, tol=target, max_iter=max_steps, omega=omega, or_sweeps=or_sweeps)
@@ -204,8 +212,11 @@ def train(ctx, data, epochs=200, batch=1024, lr=2e-3, seed=0):
     return params, losses
 
 
-def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omega=1.7, accept="theta"):
-    """Fix U to Landau gauge from g = 1 with `method` in {"or", "plain", "learned"};
+def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omega=1.7, accept="theta",
+          member=None):
+    """Fix U to Landau gauge from g = 1 with `method` in {"or", "plain",
+    "learned", "fixed"} ("fixed": the family member (alpha, high) given as
+    `member`);
     Fourier-accelerated steps are accepted on `accept` ("theta" or
     "functional"); returns dict(seconds, iterations, fallbacks, theta, functional)."""
     import torch
@@ -224,6 +235,9 @@ def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omeg
         fa.set_accept(accept == "functional")
         if method == "plain":
             fa.set_plain(PLAIN_ALPHA)
+        elif method == "fixed":
+            p2min, p2max = fa.p2range()
+            fa.set_table(*family_table(member[0], member[1], p2min, p2max))
         else:
             fa.set_mlp(params, WIDTH, beta, bf16=True)
         it, fb, th = fa.run(g, tol=tol, max_iter=max_iter, omega=omega, or_sweeps=10)
@@ -258,12 +272,17 @@ def main():
     ap.add_argument("--json", default=None)
     ap.add_argument("--sample-decades", type=int, default=0,
                     help="search this many random decades per configuration (0: every decade)")
+    ap.add_argument("--accept", choices=["theta", "functional"], default="theta",
+                    help="acceptance test of the Fourier-accelerated steps (survey, train, compare)")
+    ap.add_argument("--alphas", default=None, help="train: comma-separated step sizes of the family search")
+    ap.add_argument("--highs", default=None, help="train: comma-separated high-mode factors of the family search")
+    ap.add_argument("--fixed", default="0.08,0.35", help="compare: the fixed family member alpha,high")
     args = ap.parse_args()
     ctx = Context(0)
     if args.mode == "survey":
         members = [(a, h, b) for a in (0.06, 0.08, 0.1, 0.12) for h in (1.0, 0.6, 0.35) for b in (1.0, 2.0)]
         seeds = list(range(args.seed0, args.seed0 + args.configs))
-        res = survey(ctx, args.L, seeds, members, therm=args.therm)
+        res = survey(ctx, args.L, seeds, members, therm=args.therm, accept=args.accept)
         for c, m, v in sorted((float(np.mean([x[2] for x in v])), m, v) for m, v in res.items()):
             print(json.dumps({"alpha": m[0], "high": m[1], "low": m[2], "mean_cost": c, "cost": [x[2] for x in v],
                               "fallbacks": [x[1] for x in v]}))
@@ -283,7 +302,9 @@ def main():
             sample = None
             if args.sample_decades:
                 sample = set(int(x) for x in rng.choice(12, args.sample_decades, replace=False))
-            data.append(collect(ctx, U, beta, sample=sample))
+            alphas = tuple(float(x) for x in args.alphas.split(",")) if args.alphas else None
+            highs = tuple(float(x) for x in args.highs.split(",")) if args.highs else None
+            data.append(collect(ctx, U, beta, sample=sample, accept=args.accept, alphas=alphas, highs=highs))
             print(json.dumps({"config": k, "beta": beta, "collect_cost": collect.last_cost, "decades": collect.log,
                               "rows": int(len(data[-1]))}), flush=True)
         data = np.concatenate(data)
@@ -291,7 +312,7 @@ def main():
         params, losses = train(ctx, data)
         np.savez(args.out, params=params, gamma=1.0, width=WIDTH, samples=len(data),
                  final_loss=float(losses[-1]), first_loss=float(losses[0]), configs=ncfg, lattice=args.L,
-                 betas=betas)
+                 betas=betas, accept=args.accept)
         # the same parameters as raw little-endian FP32 for C and C++ callers
         np.asarray(params, dtype="<f4").tofile(os.path.splitext(args.out)[0] + ".f32")
         print(json.dumps({"samples": int(len(data)), "final_loss": float(losses[-1]),
@@ -302,15 +323,17 @@ def main():
         seeds = np.arange(1, args.eval_configs + 1)
         cfgs = hmc_configs(ctx, args.eval_L, [6.0] * len(seeds), seeds, args.eval_therm, 1, 0)
         rows = []
+        fixed = tuple(float(x) for x in args.fixed.split(","))
+        methods = ("or", "plain", "fixed", "learned")
         for k, (beta, Uh) in enumerate(cfgs):
-            for method in ("or", "plain", "learned"):
+            for method in methods:
                 U = prepared_links(ctx, Uh, transform_seed=5)
-                r = solve(ctx, U, method, params, beta)
+                r = solve(ctx, U, method, params, beta, accept=args.accept, member=fixed)
                 r["config"] = k
                 rows.append(r)
                 print(json.dumps(r), flush=True)
-        summ = {}
-        for m in ("or", "plain", "learned"):
+        summ = {"accept": args.accept, "fixed_member": fixed}
+        for m in methods:
             rs = [r for r in rows if r["method"] == m]
             summ[m] = {"mean_seconds": float(np.mean([r["seconds"] for r in rs])),
                        "mean_iterations": float(np.mean([r["iterations"] for r in rs])),
@@ -318,6 +341,7 @@ def main():
                        "max_theta": float(max(r["theta"] for r in rs))}
         summ["speedup_learned_vs_or"] = summ["or"]["mean_seconds"] / summ["learned"]["mean_seconds"]
         summ["speedup_learned_vs_plain"] = summ["plain"]["mean_seconds"] / summ["learned"]["mean_seconds"]
+        summ["speedup_learned_vs_fixed"] = summ["fixed"]["mean_seconds"] / summ["learned"]["mean_seconds"]
         print(json.dumps(summ))
         if args.json:
             with open(args.json, "w") as fh:
