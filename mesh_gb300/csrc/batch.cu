@@ -11,7 +11,11 @@
 // Work decomposition: the items of a launch (links: 4 planes of V_r per
 // replica, or sites: one plane of V_r) are cut into chunks of 256 items that
 // never straddle two planes or two replicas (a plane has ceil(V_r/256)
-// chunks), so a thread finds its direction and site without a division.
+// chunks). Where every extent of a replica is a multiple of 4, a chunk is a
+// 4x4x4x4 tile of sites (tiles in lexicographic order, sites of a tile
+// lexicographic), so that the neighbours a thread reads are mostly sites of
+// its own block, as in the single lattice's tiled kernels; otherwise a chunk
+// is 256 consecutive sites of the even/odd order.
 // The persistent grid walks the chunks grid-stride, so all blocks sweep the
 // batch together and neighbouring links are shared in L2. A block's replica
 // changes only at chunk boundaries (a block-uniform event), which is where
@@ -39,6 +43,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <limits>
 #include <vector>
 
@@ -58,6 +63,7 @@ struct BatchRep
 	uint64_t seed; // Philox key of the replica's momentum and Metropolis streams
 	int64_t lchunk0, schunk0; // first chunk of the replica's links / sites
 	int32_t cpp;              // chunks per plane: ceil(V / 256)
+	int32_t tile;             // 1: a chunk is a 4^4 tile of sites (every extent a multiple of 4)
 };
 
 // one item space (links or sites) of a batch and its persistent grid
@@ -95,6 +101,21 @@ __device__ __forceinline__ int find_rep(BatchSpace const &sp, int64_t c)
 			hi = mid - 1;
 	}
 	return lo;
+}
+
+// a replica is walked in 4^4 tiles when every extent is a multiple of 4
+// (MESH_BATCH_TILES=0 in the environment keeps the even/odd chunk order, for
+// comparisons)
+bool tiles_ok(int32_t const *d)
+{
+	static_assert(kChunk == 256, "a tile of 4^4 sites is one chunk");
+	char const *e = std::getenv("MESH_BATCH_TILES");
+	if (e && e[0] == '0')
+		return false;
+	for (int i = 0; i < kBND; ++i)
+		if (d[i] % 4 != 0)
+			return false;
+	return true;
 }
 
 // sum over the block (valid in thread 0); every thread must call it
@@ -156,9 +177,30 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 		touched = true;
 		uint32_t local = uint32_t(c - first);
 		uint32_t mu = local / uint32_t(rep.cpp);
-		int64_t s = int64_t(local - mu * uint32_t(rep.cpp)) * kChunk + threadIdx.x;
-		if (s < rep.g.V)
-			acc += body(r, rep, int(mu), s);
+		uint32_t k = local - mu * uint32_t(rep.cpp);
+		if (rep.tile)
+		{
+			// tile k of the replica, site threadIdx.x of the tile
+			int x[kBND];
+			uint32_t t = k, a = threadIdx.x;
+#pragma unroll
+			for (int i = kBND - 1; i >= 0; --i)
+			{
+				uint32_t n = uint32_t(rep.g.L[i]) >> 2;
+				uint32_t q = t / n;
+				x[i] = int((t - q * n) << 2) + int(a & 3u);
+				t = q;
+				a >>= 2;
+			}
+			Site<kBND> st = site_from_coords<kBND>(rep.g, x);
+			acc += body(r, rep, int(mu), eo_of<kBND>(rep.g, st), st);
+		}
+		else
+		{
+			int64_t s = int64_t(k) * kChunk + threadIdx.x;
+			if (s < rep.g.V)
+				acc += body(r, rep, int(mu), s, site_from_eo<kBND>(rep.g, s));
+		}
 	}
 	if constexpr (RED)
 	{
@@ -199,8 +241,7 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 template <int GRP, class T> __global__ void __launch_bounds__(kChunk) kb_random_links(BatchSpace sp)
 {
 	using Gp = Group<GRP, T>;
-	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s) {
-		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &st) {
 		T p[Gp::NNORM_GROUP];
 		normals<T, Gp::NNORM_GROUP>(rep.seed, TAG_GAUGE, uint32_t(st.lex), uint32_t(mu), 0, p);
 		auto e = Gp::group_from_normals(p);
@@ -212,7 +253,7 @@ template <int GRP, class T> __global__ void __launch_bounds__(kChunk) kb_random_
 template <int GRP, class T> __global__ void __launch_bounds__(kChunk) kb_unit_links(BatchSpace sp)
 {
 	using Gp = Group<GRP, T>;
-	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s) {
+	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &) {
 		auto e = Gp::unit();
 		comp<T, Gp::NR>(static_cast<T *>(rep.U), rep.g.V, mu).store(s, e.v);
 		return 0.0;
@@ -225,8 +266,7 @@ template <int GRP, class T>
 __global__ void __launch_bounds__(kChunk) kb_refresh(BatchSpace sp, HmcDev const *__restrict__ dev, BatchRed kin)
 {
 	using Gp = Group<GRP, T>;
-	batch_loop<true>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s) {
-		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+	batch_loop<true>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &st) {
 		T p[Gp::DIM], o[Gp::NA];
 		normals<T, Gp::DIM>(rep.seed, TAG_MOMENTUM, uint32_t(st.lex), uint32_t(mu), dev[r].traj, p);
 		Gp::alg_from_normals(p, o);
@@ -241,7 +281,7 @@ __global__ void __launch_bounds__(kChunk) kb_evolve(BatchSpace sp, T t)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
-	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s) {
+	batch_loop<false>(sp, BatchRed{}, [&](int, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &) {
 		int64_t V = rep.g.V;
 		T p[Gp::NA];
 		comp<T, Gp::NA>(static_cast<T *>(rep.P), V, mu).load(s, p);
@@ -268,9 +308,8 @@ __global__ void __launch_bounds__(kChunk)
     kb_force(BatchSpace sp, double const *__restrict__ beta, double delta, BatchRed kin)
 {
 	using Gp = Group<GRP, T>;
-	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s) {
+	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &st) {
 		int64_t V = rep.g.V;
-		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(rep.Unew), V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * delta);
 		double k = force_item<GRP, T, kBND>(rep.g, st, s, mu, ld, static_cast<T *>(rep.P), coef);
@@ -287,8 +326,7 @@ __global__ void __launch_bounds__(kChunk)
 {
 	using Gp = Group<GRP, T>;
 	constexpr int F2 = (GRP == SU3 && sizeof(T) == 4) ? 1 : 0;
-	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s) {
-		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(flip ? rep.Ut : rep.Unew), rep.g.V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
 		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true>(rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
@@ -312,8 +350,7 @@ __global__ void kb_swap_proposal(BatchRep *reps, int R)
 // per-replica plaquette trace sums of U (NEW: of U_new)
 template <int GRP, class T, bool NEW> __global__ void __launch_bounds__(kChunk) kb_plaquette(BatchSpace sp, BatchRed out)
 {
-	batch_loop<true>(sp, out, [&](int, BatchRep const &rep, int, int64_t s) {
-		Site<kBND> st = site_from_eo<kBND>(rep.g, s);
+	batch_loop<true>(sp, out, [&](int, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(NEW ? rep.Unew : rep.U), rep.g.V};
 		return double(plaquette_site<GRP, T, kBND>(rep.g, st, s, ld));
 	});
@@ -723,6 +760,7 @@ int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t
 			rep.lchunk0 = lch;
 			rep.schunk0 = sch;
 			rep.cpp = int32_t((V + kChunk - 1) / kChunk);
+			rep.tile = tiles_ok(dims + size_t(r) * kBND) ? 1 : 0;
 			lch += int64_t(kBND) * rep.cpp;
 			sch += rep.cpp;
 			offU[r] = totU;

@@ -1631,11 +1631,11 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 0, 3, 4}, 128, 4, "site/tile1x1x8x16/128thr/4blk/f32x2", 1},
 		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2", 1},
-		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk"},
-		    {3, {0, 0, 0, 0}, 256, 2, "line/256thr/2blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/row2", 1, 1},
 		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2", 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2", 1, 1},
-		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2/row2", 1, 1}};
+		    {3, {0, 0, 0, 0}, 64, 6, "line/64thr/6blk/f32x2/row2", 1, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1762,15 +1762,16 @@ template <int GRP, class T, int ND> struct Ops
 			LineSpec ls{};
 			ls.ns = 32 / g.L[3];
 			ls.ncol = g.L[0] * (g.L[2] / ls.ns);
-			ls.items = int64_t(ls.ncol) * g.L[1];
 			// FP64 slots take twice the shared memory: 64-thread blocks
 			int threads = sizeof(T) == 8 ? 64 : fv.threads;
 			int minb = sizeof(T) == 8 ? 6 : fv.minb;
 			int wpb = threads / 32;
-			int64_t need = (ls.items + wpb - 1) / wpb;
-			int64_t cap = int64_t(c.num_sms) * minb;
-			unsigned b = unsigned(need < cap ? need : cap);
-			ls.nwarps = int64_t(b) * wpb;
+			// segments of the x1 march: as many as the resident warps allow
+			int64_t resident = int64_t(c.num_sms) * minb * wpb;
+			int64_t nseg = resident / ls.ncol;
+			ls.nseg = int(nseg < 1 ? 1 : (nseg > g.L[1] ? g.L[1] : nseg));
+			ls.nwork = ls.ncol * ls.nseg;
+			unsigned b = unsigned((ls.nwork + wpb - 1) / wpb);
 			if constexpr (sizeof(T) == 8)
 				k_md_line<T, 64, 6, 0, ROWS, FUSE><<<b, 64, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
 			else
@@ -1786,25 +1787,28 @@ template <int GRP, class T, int ND> struct Ops
 	static void line_cfg(ForceVariant const &fv, unsigned b, Geom const &g, LineSpec const &ls, T const *u, T *p,
 	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
 	{
+		auto go = [&](auto kernel, int threads) {
+			kernel<<<b, threads, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+		};
 		if constexpr (ROWS && F2)
 		{
 			if (fv.r2)
 			{
-				if (fv.minb == 3)
-					k_md_line<T, 128, 3, F2, ROWS, FUSE, true>
-					    <<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+				if (fv.threads == 64 && fv.minb == 6)
+					go(k_md_line<T, 64, 6, F2, ROWS, FUSE, true>, 64);
+				else if (fv.threads == 64)
+					go(k_md_line<T, 64, 8, F2, ROWS, FUSE, true>, 64);
 				else
-					k_md_line<T, 128, 4, F2, ROWS, FUSE, true>
-					    <<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+					go(k_md_line<T, 128, 4, F2, ROWS, FUSE, true>, 128);
 				return;
 			}
 		}
-		if (fv.threads == 256)
-			k_md_line<T, 256, 2, F2, ROWS, FUSE><<<b, 256, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+		if (fv.threads == 64)
+			go(k_md_line<T, 64, 8, F2, ROWS, FUSE>, 64);
 		else if (fv.minb == 3)
-			k_md_line<T, 128, 3, F2, ROWS, FUSE><<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+			go(k_md_line<T, 128, 3, F2, ROWS, FUSE>, 128);
 		else
-			k_md_line<T, 128, 4, F2, ROWS, FUSE><<<b, 128, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
+			go(k_md_line<T, 128, 4, F2, ROWS, FUSE>, 128);
 	}
 	// tiles of variant fv over g and the grid size (at most minb blocks per SM)
 	static TileSpec tiles_for(Geom const &g, ForceVariant const &fv, Context const &c, unsigned &b)

@@ -29,11 +29,12 @@
 // site reads its own four links, the twelve forward neighbours
 // U_nu(x + mu) and the links of the x0 and x2 lower staples.
 //
-// Work assignment: "columns" of lines (x0, x2-group) times x1 form a list of
-// L0 (L2 ns / 32...) line steps in column-major order; every warp of the
-// persistent grid takes one contiguous range of it, so all warps hold the
-// same number of steps to within one. At the first step of a range, and when
-// a range passes into the next column, the carry along x1 is computed for the
+// Work assignment: a "column" is the set of lines (x0, x2-group) along x1;
+// its x1 march is cut into nseg segments, and every warp of the launch takes
+// one (column, segment), warp w the column w mod ncol, so that the warps of
+// a block hold neighbouring columns and all warps march in step: the lines
+// being read at one time are a few x1 slices of the lattice, which stay in
+// L2. At the first step of a segment the carry along x1 is computed for the
 // line behind (three plaquettes and their contributions).
 //
 // The sum runs in a different order than the reference's staple sum, which
@@ -47,10 +48,10 @@ namespace meshgb {
 
 struct LineSpec
 {
-	int ns;         // lines per warp = 32 / L3
-	int ncol;       // columns = L0 * L2 / ns
-	int64_t items;  // line steps = ncol * L1
-	int64_t nwarps; // warps of the launch
+	int ns;   // lines per warp = 32 / L3
+	int ncol; // columns of lines along x1: L0 * L2 / ns
+	int nseg; // segments of the x1 march per column
+	int nwork; // warps with work: ncol * nseg
 };
 
 inline bool line_supported(Geom const &g)
@@ -202,34 +203,89 @@ template <class T, int F2> struct LineProd
 // with row 2 rebuilt from rows 0, 1 (R2 = false: 48 bytes read, 24 FMAs) or
 // read from memory (R2 = true: 72 bytes, no arithmetic). FP64 links and
 // ROWS = false read every real.
-template <class T, bool ROWS, bool R2> struct LineLoad
+template <class T, bool ROWS, bool R2> struct LineLoad;
+template <bool ROWS, bool R2> struct LineLoad<float, ROWS, R2>
 {
-	using Gp = Group<SU3, T>;
+	// component mu: float4 planes k = 0..3 at mu 9 V/2 + k V (in float4
+	// units), the float2 plane at mu 9 V + 8 V (in float2 units); 32-bit
+	// indices (the library keeps 72 V < 2^32 reals per field)
+	using Gp = Group<SU3, float>;
 	using E = typename Gp::E;
-	T const *U;
-	int64_t V;
-	__device__ __forceinline__ E operator()(int mu, int64_t s) const
+	float const *U;
+	uint32_t V;
+	__device__ __forceinline__ void head(int mu, uint32_t s, E &e) const
+	{
+		float4 const *p = reinterpret_cast<float4 const *>(U) + (uint32_t(mu) * 9u * (V >> 1) + s);
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			float4 t = ld4<CACHE_KEEP>(p + k * V);
+			e.v[4 * k] = t.x;
+			e.v[4 * k + 1] = t.y;
+			e.v[4 * k + 2] = t.z;
+			e.v[4 * k + 3] = t.w;
+		}
+	}
+	__device__ __forceinline__ E operator()(int mu, uint32_t s) const
 	{
 		E e;
+		head(mu, s, e);
 		if constexpr (ROWS && !R2)
-		{
-			Soa<T, 18>::template load_head<12, CACHE_KEEP>(U + int64_t(mu) * 18 * V, V, s, e.v);
 			Gp::complete_row2(e);
-		}
 		else
-			Soa<T, 18>::template load<CACHE_KEEP>(U + int64_t(mu) * 18 * V, V, s, e.v);
+		{
+			float4 t = ld4<CACHE_KEEP>(reinterpret_cast<float4 const *>(U) + (uint32_t(mu) * 9u * (V >> 1) + 3 * V + s));
+			e.v[12] = t.x;
+			e.v[13] = t.y;
+			e.v[14] = t.z;
+			e.v[15] = t.w;
+			float2 u = ld2<CACHE_KEEP>(reinterpret_cast<float2 const *>(U) + (uint32_t(mu) * 9u * V + 8 * V + s));
+			e.v[16] = u.x;
+			e.v[17] = u.y;
+		}
 		return e;
 	}
-	__device__ __forceinline__ E rows(int mu, int64_t s) const
+	__device__ __forceinline__ E rows(int mu, uint32_t s) const
 	{
 		if constexpr (ROWS)
 		{
 			E e;
-			Soa<T, 18>::template load_head<12, CACHE_KEEP>(U + int64_t(mu) * 18 * V, V, s, e.v);
+			head(mu, s, e);
 			return e;
 		}
 		else
 			return (*this)(mu, s);
+	}
+};
+template <bool ROWS, bool R2> struct LineLoad<double, ROWS, R2>
+{
+	// component mu: double2 planes k = 0..8 at mu 9 V + k V
+	using Gp = Group<SU3, double>;
+	using E = typename Gp::E;
+	double const *U;
+	uint32_t V;
+	template <int K> __device__ __forceinline__ void planes(int mu, uint32_t s, E &e) const
+	{
+		double2 const *p = reinterpret_cast<double2 const *>(U) + (uint32_t(mu) * 9u * V + s);
+#pragma unroll
+		for (int k = 0; k < K; ++k)
+		{
+			double2 t = ld2d<CACHE_KEEP>(p + k * V);
+			e.v[2 * k] = t.x;
+			e.v[2 * k + 1] = t.y;
+		}
+	}
+	__device__ __forceinline__ E operator()(int mu, uint32_t s) const
+	{
+		E e;
+		planes<9>(mu, s, e);
+		return e;
+	}
+	__device__ __forceinline__ E rows(int mu, uint32_t s) const
+	{
+		E e;
+		planes<6>(mu, s, e);
+		return e;
 	}
 };
 
@@ -246,15 +302,15 @@ __device__ __forceinline__ int wrap_add(int x, int d, int L)
 }
 
 // even/odd index of the site (a0, a1, a2, a3) (coordinates in range)
-__device__ __forceinline__ int64_t line_eo(Geom const &g, int a0, int a1, int a2, int a3)
+__device__ __forceinline__ uint32_t line_eo(Geom const &g, int a0, int a1, int a2, int a3)
 {
-	int32_t lex = ((a0 * g.L[1] + a1) * g.L[2] + a2) * g.L[3] + a3;
-	int p = (a0 + a1 + a2 + a3) & 1;
-	return int64_t(p) * g.Vh + (lex >> 1);
+	uint32_t lex = uint32_t(((a0 * g.L[1] + a1) * g.L[2] + a2) * g.L[3] + a3);
+	uint32_t p = uint32_t(a0 + a1 + a2 + a3) & 1u;
+	return p * uint32_t(g.Vh) + (lex >> 1);
 }
 
 // site x shifted by s1 along d1 and s2 along d2 (s = 0: no shift)
-__device__ __forceinline__ int64_t line_nb(Geom const &g, LineSite const &x, int d1, int s1, int d2 = 0, int s2 = 0)
+__device__ __forceinline__ uint32_t line_nb(Geom const &g, LineSite const &x, int d1, int s1, int d2 = 0, int s2 = 0)
 {
 	int c[4] = {x.x0, x.x1, x.x2, x.x3};
 #pragma unroll
@@ -266,9 +322,78 @@ __device__ __forceinline__ int64_t line_nb(Geom const &g, LineSite const &x, int
 	return line_eo(g, c[0], c[1], c[2], c[3]);
 }
 
+// lexicographic index after a step of `sign` along d, for coordinate xd
+__device__ __forceinline__ uint32_t lex_shift(uint32_t lex, int xd, int Ld, uint32_t str, int sign)
+{
+	if (sign > 0)
+		return xd == Ld - 1 ? lex - uint32_t(Ld - 1) * str : lex + str;
+	return xd == 0 ? lex + uint32_t(Ld - 1) * str : lex - str;
+}
+
+// even/odd indices of the neighbours one step of the march reads, computed
+// once per site: x + e_mu, x - e_0, x - e_2 and x - e_nu + e_mu (nu = 0, 2)
+struct LineNb
+{
+	uint32_t f[4];                // x + e_mu (opposite parity)
+	uint32_t b0, b2;              // x - e_0, x - e_2 (opposite parity)
+	uint32_t d01, d02, d03;       // x - e_0 + e_mu, mu = 1, 2, 3 (x's parity)
+	uint32_t d20, d21, d23;       // x - e_2 + e_mu, mu = 0, 1, 3
+	// selects on constant members (a runtime index into f would go to local memory)
+	__device__ __forceinline__ uint32_t fwd(int mu) const
+	{
+		return mu == 0 ? f[0] : mu == 1 ? f[1] : mu == 2 ? f[2] : f[3];
+	}
+	__device__ __forceinline__ uint32_t diag(int nu, int mu) const
+	{
+		if (nu == 0)
+			return mu == 1 ? d01 : mu == 2 ? d02 : d03;
+		return mu == 0 ? d20 : mu == 1 ? d21 : d23;
+	}
+};
+
+__device__ __forceinline__ LineNb line_neighbours(Geom const &g, LineSite const &x)
+{
+	int c[4] = {x.x0, x.x1, x.x2, x.x3};
+	uint32_t str[4] = {uint32_t(g.stride[0]), uint32_t(g.stride[1]), uint32_t(g.stride[2]), uint32_t(g.stride[3])};
+	uint32_t lex = ((uint32_t(c[0]) * g.L[1] + c[1]) * g.L[2] + c[2]) * g.L[3] + c[3];
+	uint32_t par = uint32_t(c[0] + c[1] + c[2] + c[3]) & 1u;
+	uint32_t Vh = uint32_t(g.Vh);
+	uint32_t po = (par ^ 1u) * Vh, ps = par * Vh;
+	LineNb n;
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+		n.f[mu] = po + (lex_shift(lex, c[mu], g.L[mu], str[mu], +1) >> 1);
+	uint32_t y0 = lex_shift(lex, c[0], g.L[0], str[0], -1);
+	uint32_t y2 = lex_shift(lex, c[2], g.L[2], str[2], -1);
+	n.b0 = po + (y0 >> 1);
+	n.b2 = po + (y2 >> 1);
+	n.d01 = ps + (lex_shift(y0, c[1], g.L[1], str[1], +1) >> 1);
+	n.d02 = ps + (lex_shift(y0, c[2], g.L[2], str[2], +1) >> 1);
+	n.d03 = ps + (lex_shift(y0, c[3], g.L[3], str[3], +1) >> 1);
+	n.d20 = ps + (lex_shift(y2, c[0], g.L[0], str[0], +1) >> 1);
+	n.d21 = ps + (lex_shift(y2, c[1], g.L[1], str[1], +1) >> 1);
+	n.d23 = ps + (lex_shift(y2, c[3], g.L[3], str[3], +1) >> 1);
+	return n;
+}
+
+// A = proj of the plaquette (mu, nu) at site x (mu < nu, runtime) from the
+// forward neighbours x + e_mu (fmu) and x + e_nu (fnu)
+template <class T, int F2, class LD>
+__device__ __forceinline__ void plaquette_at(uint32_t s, uint32_t fmu, uint32_t fnu, int mu, int nu, LD const &ld,
+                                             T *o)
+{
+	using Pr = LineProd<T, F2>;
+	using Gp = Group<SU3, T>;
+	using E = typename Gp::E;
+	E M1 = Pr::mul01(ld.rows(mu, s), ld(nu, fmu));
+	E M2 = Pr::mul01(ld.rows(nu, s), ld(mu, fnu));
+	Gp::complete_row2(M2);
+	Pr::proj01(Pr::mul01_nd(M1, M2), o);
+}
+
 // A = proj of the plaquette (mu, nu) at site x (mu < nu, runtime)
 template <class T, int F2, class LD>
-__device__ __forceinline__ void line_plaquette(Geom const &g, LineSite const &x, int64_t s, int mu, int nu,
+__device__ __forceinline__ void line_plaquette(Geom const &g, LineSite const &x, uint32_t s, int mu, int nu,
                                                LD const &ld, T *o)
 {
 	using Pr = LineProd<T, F2>;
@@ -353,7 +478,7 @@ __device__ __forceinline__ void line_carry(Geom const &g, LineSite const &x, LD 
 	using E = typename Gp::E;
 	LineSite y = x;
 	y.x1 = wrap_add(x.x1, -1, g.L[1]);
-	int64_t sy = line_eo(g, y.x0, y.x1, y.x2, y.x3);
+	uint32_t sy = line_eo(g, y.x0, y.x1, y.x2, y.x3);
 #pragma unroll 1
 	for (int k = 0; k < 3; ++k)
 	{
@@ -384,28 +509,29 @@ __global__ void __launch_bounds__(NT, MINB)
 	// per warp: hand-over along x3 (3 links) and the carry along x1 (3 links)
 	__shared__ SW sm_x3[NW][NS];
 	__shared__ SW sm_x1[NW][NS];
-	LineLoad<T, ROWS, R2> ld{U, g.V};
+	LineLoad<T, ROWS, R2> ld{U, uint32_t(g.V)};
 	int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	SW *s3 = sm_x3[wib];
 	SW *s1 = sm_x1[wib];
-	int64_t wid = int64_t(blockIdx.x) * NW + wib;
-	int64_t i0 = wid * ls.items / ls.nwarps, i1 = (wid + 1) * ls.items / ls.nwarps;
+	int wid = int(blockIdx.x) * NW + wib;
 	int L1 = g.L[1], L3 = g.L[3];
 	int sub = lane / L3;
 	int lane_prev = sub * L3 + (lane % L3 == 0 ? L3 - 1 : lane % L3 - 1);
 	int ngrp = g.L[2] / ls.ns;
+	int col = wid % ls.ncol, seg = wid / ls.ncol;
+	int t0 = seg * L1 / ls.nseg, t1 = wid < ls.nwork ? (seg + 1) * L1 / ls.nseg : t0;
 	double acc = 0.0;
-	for (int64_t it = i0; it < i1; ++it)
+	for (int t = t0; t < t1; ++t)
 	{
-		int col = int(it / L1);
 		LineSite x;
-		x.x1 = int(it - int64_t(col) * L1);
+		x.x1 = t;
 		x.x0 = col / ngrp;
 		x.x2 = (col - x.x0 * ngrp) * ls.ns + sub;
 		x.x3 = lane % L3;
-		int64_t s = line_eo(g, x.x0, x.x1, x.x2, x.x3);
-		if (it == i0 || x.x1 == 0)
+		uint32_t s = line_eo(g, x.x0, x.x1, x.x2, x.x3);
+		if (t == t0)
 			line_carry<T, F2>(g, x, ld, s1, lane);
+		LineNb nb = line_neighbours(g, x);
 		T F[4][NA];
 		// the carry from x - e_1: links 0, 2, 3
 #pragma unroll
@@ -421,7 +547,7 @@ __global__ void __launch_bounds__(NT, MINB)
 		{
 			int mu = plane_mu<4>(q), nu = plane_nu<4>(q);
 			T o[8];
-			line_plaquette<T, F2>(g, x, s, mu, nu, ld, o);
+			plaquette_at<T, F2>(s, nb.fwd(mu), nb.fwd(nu), mu, nu, ld, o);
 			add_plane<4, NA>(F, q, o);
 			// hand-overs: along x1 (planes with mu or nu = 1), along x3 (nu = 3)
 #pragma unroll 1
@@ -454,8 +580,8 @@ __global__ void __launch_bounds__(NT, MINB)
 				int nu = r == 0 ? 0 : 2;
 				if (nu == mu)
 					continue;
-				int64_t y = line_nb(g, x, nu, -1);
-				E f = ld(nu, line_nb(g, x, nu, -1, mu, +1));
+				uint32_t y = nu == 0 ? nb.b0 : nb.b2;
+				E f = ld(nu, nb.diag(nu, mu));
 				E ef = PrO::mul_r2(ld.rows(mu, y), f);
 				Gp::add_to(S, PrO::mul_dn(ef, ld(nu, y)));
 			}
