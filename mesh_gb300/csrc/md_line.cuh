@@ -150,6 +150,34 @@ template <class T, int F2> struct LineProd
 		o[6] = (p.v[10] - p21.re) * T(0.5);
 		o[7] = (p.v[11] + p21.im) * T(0.5);
 	}
+	// proj(a b) (antihermitian traceless part, packed) from the nine entries
+	// of the product it needs
+	__device__ __forceinline__ static void proj_mul(E const &a, E const &b, T *o)
+	{
+		auto c = [&](int i, int j) {
+			cx<T> z = cmul(a.at(i, 0), b.at(0, j));
+			z = cadd(z, cmul(a.at(i, 1), b.at(1, j)));
+			return cadd(z, cmul(a.at(i, 2), b.at(2, j)));
+		};
+		auto ci = [&](int i) {
+			T z = T(0);
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+				z += a.v[6 * i + 2 * k] * b.v[6 * k + 2 * i + 1] + a.v[6 * i + 2 * k + 1] * b.v[6 * k + 2 * i];
+			return z;
+		};
+		T i0 = ci(0), i1 = ci(1), i2 = ci(2);
+		T t = (i0 + i1 + i2) * T(1.0 / 3.0);
+		cx<T> c01 = c(0, 1), c10 = c(1, 0), c02 = c(0, 2), c20 = c(2, 0), c12 = c(1, 2), c21 = c(2, 1);
+		o[0] = i0 - t;
+		o[1] = i1 - t;
+		o[2] = (c01.re - c10.re) * T(0.5);
+		o[3] = (c01.im + c10.im) * T(0.5);
+		o[4] = (c02.re - c20.re) * T(0.5);
+		o[5] = (c02.im + c20.im) * T(0.5);
+		o[6] = (c12.re - c21.re) * T(0.5);
+		o[7] = (c12.im + c21.im) * T(0.5);
+	}
 	// sg V^+ A V for A = from_alg(o) and unitary V, packed (upper triangle
 	// and the imaginary diagonal of the exactly antihermitian traceless
 	// result)
@@ -585,9 +613,8 @@ __global__ void __launch_bounds__(NT, MINB)
 				E ef = PrO::mul_r2(ld.rows(mu, y), f);
 				Gp::add_to(S, PrO::mul_dn(ef, ld(nu, y)));
 			}
-			E W = PrO::mul(ld(mu, s), S);
 			T xa[NA];
-			Gp::proj(W, xa);
+			Pr::proj_mul(ld(mu, s), S, xa);
 			add_link<NA>(F, mu, xa);
 		}
 		// contributions from x - e_3 (the previous lane): links 0, 1, 2

@@ -280,7 +280,10 @@ def main():
     args = ap.parse_args()
     ctx = Context(0)
     if args.mode == "survey":
-        members = [(a, h, b) for a in (0.06, 0.08, 0.1, 0.12) for h in (1.0, 0.6, 0.35) for b in (1.0, 2.0)]
+        alphas = tuple(float(x) for x in args.alphas.split(",")) if args.alphas else (0.06, 0.08, 0.1, 0.12)
+        highs = tuple(float(x) for x in args.highs.split(",")) if args.highs else (1.0, 0.6, 0.35)
+        lows = (1.0,) if args.alphas else (1.0, 2.0)
+        members = [(a, h, b) for a in alphas for h in highs for b in lows]
         seeds = list(range(args.seed0, args.seed0 + args.configs))
         res = survey(ctx, args.L, seeds, members, therm=args.therm, accept=args.accept)
         for c, m, v in sorted((float(np.mean([x[2] for x in v])), m, v) for m, v in res.items()):
