@@ -1587,6 +1587,7 @@ template <int GRP, class T, int ND> struct Ops
 		char const *name;
 		int f2 = 0;        // packed FP32x2 products (SU(3) float only)
 		int r2 = 0;        // line march: row 2 of whole-link loads read, not rebuilt
+		int fsm = 0;       // line march: force accumulators in shared memory
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1633,9 +1634,9 @@ template <int GRP, class T, int ND> struct Ops
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2", 1},
 		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2", 1},
 		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/row2", 1, 1},
-		    {3, {0, 0, 0, 0}, 128, 3, "line/128thr/3blk/f32x2", 1},
+		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/fsm", 1, 0, 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2", 1, 1},
-		    {3, {0, 0, 0, 0}, 64, 6, "line/64thr/6blk/f32x2/row2", 1, 1}};
+		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/row2/fsm", 1, 1, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1792,11 +1793,17 @@ template <int GRP, class T, int ND> struct Ops
 		};
 		if constexpr (ROWS && F2)
 		{
+			if (fv.fsm)
+			{
+				if (fv.r2)
+					go(k_md_line<T, 128, 5, F2, ROWS, FUSE, true, true>, 128);
+				else
+					go(k_md_line<T, 128, 5, F2, ROWS, FUSE, false, true>, 128);
+				return;
+			}
 			if (fv.r2)
 			{
-				if (fv.threads == 64 && fv.minb == 6)
-					go(k_md_line<T, 64, 6, F2, ROWS, FUSE, true>, 64);
-				else if (fv.threads == 64)
+				if (fv.threads == 64)
 					go(k_md_line<T, 64, 8, F2, ROWS, FUSE, true>, 64);
 				else
 					go(k_md_line<T, 128, 4, F2, ROWS, FUSE, true>, 128);

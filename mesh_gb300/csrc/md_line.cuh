@@ -495,6 +495,54 @@ template <int NA, class T> __device__ __forceinline__ void add_link(T (&F)[4][NA
 		}
 }
 
+// the force accumulators F[mu] (8 reals for each of the four links of a
+// site): in registers, or (FSM) in shared-memory slots of the thread, which
+// frees 32 registers for a higher occupancy
+template <class T, bool FSM> struct FAcc;
+template <class T> struct FAcc<T, false>
+{
+	T F[4][8];
+	__device__ __forceinline__ FAcc(typename Slot16<T>::W *, int) {}
+	__device__ __forceinline__ void set(int k, T const *o)
+	{
+#pragma unroll
+		for (int j = 0; j < 4; ++j)
+			if (j == k)
+#pragma unroll
+				for (int a = 0; a < 8; ++a)
+					F[j][a] = o[a];
+	}
+	__device__ __forceinline__ void add(int k, T const *o, T sg) { add_link<8>(F, k, o, sg); }
+	__device__ __forceinline__ void get(int k, T *o) const
+	{
+#pragma unroll
+		for (int a = 0; a < 8; ++a)
+		{
+			o[a] = F[0][a];
+#pragma unroll
+			for (int j = 1; j < 4; ++j)
+				o[a] = k == j ? F[j][a] : o[a];
+		}
+	}
+};
+template <class T> struct FAcc<T, true>
+{
+	typename Slot16<T>::W *sl;
+	int lane;
+	__device__ __forceinline__ FAcc(typename Slot16<T>::W *s, int l) : sl(s), lane(l) {}
+	__device__ __forceinline__ void set(int k, T const *o) { slot_store<T>(sl, k, lane, o); }
+	__device__ __forceinline__ void add(int k, T const *o, T sg)
+	{
+		T f[8];
+		slot_load<T>(sl, k, lane, f);
+#pragma unroll
+		for (int a = 0; a < 8; ++a)
+			f[a] += sg * o[a];
+		slot_store<T>(sl, k, lane, f);
+	}
+	__device__ __forceinline__ void get(int k, T *o) const { slot_load<T>(sl, k, lane, o); }
+};
+
 // carry of the line behind x (x - e_1): the contributions of its planes
 // (0,1), (1,2), (1,3) to links 0, 2, 3 of x, into the carry slots
 template <class T, int F2, class LD>
@@ -521,7 +569,7 @@ __device__ __forceinline__ void line_carry(Geom const &g, LineSite const &x, LD 
 
 // One momentum step (and with FUSE the link update after it) of every link,
 // line-marching. P -= coef F(U); Uout = exp(tu P) U (reunitised when reunit).
-template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE, bool R2 = false>
+template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE, bool R2 = false, bool FSM = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_md_line(Geom g, LineSpec ls, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
               T *__restrict__ Uout, T tu, int reunit)
@@ -537,6 +585,8 @@ __global__ void __launch_bounds__(NT, MINB)
 	// per warp: hand-over along x3 (3 links) and the carry along x1 (3 links)
 	__shared__ SW sm_x3[NW][NS];
 	__shared__ SW sm_x1[NW][NS];
+	// FSM: the force accumulators of the warp's threads, [link][word][lane]
+	__shared__ SW sm_f[FSM ? NW : 1][FSM ? 4 * Slot16<T>::N * 32 : 1];
 	LineLoad<T, ROWS, R2> ld{U, uint32_t(g.V)};
 	int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	SW *s3 = sm_x3[wib];
@@ -560,14 +610,21 @@ __global__ void __launch_bounds__(NT, MINB)
 		if (t == t0)
 			line_carry<T, F2>(g, x, ld, s1, lane);
 		LineNb nb = line_neighbours(g, x);
-		T F[4][NA];
+		FAcc<T, FSM> F(sm_f[FSM ? wib : 0], lane);
 		// the carry from x - e_1: links 0, 2, 3
+		{
+			T z[NA], c[NA];
 #pragma unroll
-		for (int a = 0; a < NA; ++a)
-			F[1][a] = T(0);
-		slot_load<T>(s1, 0, lane, F[0]);
-		slot_load<T>(s1, 1, lane, F[2]);
-		slot_load<T>(s1, 2, lane, F[3]);
+			for (int a = 0; a < NA; ++a)
+				z[a] = T(0);
+			F.set(1, z);
+			slot_load<T>(s1, 0, lane, c);
+			F.set(0, c);
+			slot_load<T>(s1, 1, lane, c);
+			F.set(2, c);
+			slot_load<T>(s1, 2, lane, c);
+			F.set(3, c);
+		}
 		__syncwarp();
 		// the six plaquettes of x
 #pragma unroll 1
@@ -576,7 +633,8 @@ __global__ void __launch_bounds__(NT, MINB)
 			int mu = plane_mu<4>(q), nu = plane_nu<4>(q);
 			T o[8];
 			plaquette_at<T, F2>(s, nb.fwd(mu), nb.fwd(nu), mu, nu, ld, o);
-			add_plane<4, NA>(F, q, o);
+			F.add(mu, o, T(1));
+			F.add(nu, o, T(-1));
 			// hand-overs: along x1 (planes with mu or nu = 1), along x3 (nu = 3)
 #pragma unroll 1
 			for (int r = 0; r < 2; ++r)
@@ -615,7 +673,7 @@ __global__ void __launch_bounds__(NT, MINB)
 			}
 			T xa[NA];
 			Pr::proj_mul(ld(mu, s), S, xa);
-			add_link<NA>(F, mu, xa);
+			F.add(mu, xa, T(1));
 		}
 		// contributions from x - e_3 (the previous lane): links 0, 1, 2
 		__syncwarp();
@@ -625,7 +683,7 @@ __global__ void __launch_bounds__(NT, MINB)
 			for (int k = 0; k < 3; ++k)
 			{
 				slot_load<T>(s3, k, lane_prev, c);
-				add_link<NA>(F, k, c);
+				F.add(k, c, T(1));
 			}
 		}
 		__syncwarp();
@@ -634,14 +692,7 @@ __global__ void __launch_bounds__(NT, MINB)
 		for (int mu = 0; mu < 4; ++mu)
 		{
 			T f[NA];
-#pragma unroll
-			for (int a = 0; a < NA; ++a)
-			{
-				f[a] = F[0][a];
-#pragma unroll
-				for (int k = 1; k < 4; ++k)
-					f[a] = mu == k ? F[k][a] : f[a];
-			}
+			F.get(mu, f);
 			auto Pv = comp<T, NA>(P, g.V, mu);
 			T p[NA];
 			Pv.template load<CACHE_STREAM>(s, p);
