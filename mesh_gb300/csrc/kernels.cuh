@@ -1588,6 +1588,7 @@ template <int GRP, class T, int ND> struct Ops
 		int f2 = 0;        // packed FP32x2 products (SU(3) float only)
 		int r2 = 0;        // line march: row 2 of whole-link loads read, not rebuilt
 		int fsm = 0;       // line march: force accumulators in shared memory
+		int pf = 0;        // line march: L1 prefetch of the next iteration's links
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1632,11 +1633,11 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 0, 3, 4}, 128, 4, "site/tile1x1x8x16/128thr/4blk/f32x2", 1},
 		    {2, {1, 1, 1, 4}, 128, 4, "site/tile2x2x2x16/128thr/4blk/f32x2", 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2", 1},
-		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2", 1},
-		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/row2", 1, 1},
+		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/pf", 1, 0, 0, 1},
+		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/fsm/pf", 1, 0, 1, 1},
 		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/fsm", 1, 0, 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2", 1, 1},
-		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/row2/fsm", 1, 1, 1}};
+		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2/pf", 1, 1, 0, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1795,18 +1796,23 @@ template <int GRP, class T, int ND> struct Ops
 		{
 			if (fv.fsm)
 			{
-				if (fv.r2)
-					go(k_md_line<T, 128, 5, F2, ROWS, FUSE, true, true>, 128);
+				if (fv.pf)
+					go(k_md_line<T, 128, 5, F2, ROWS, FUSE, false, true, true>, 128);
 				else
 					go(k_md_line<T, 128, 5, F2, ROWS, FUSE, false, true>, 128);
 				return;
 			}
 			if (fv.r2)
 			{
-				if (fv.threads == 64)
-					go(k_md_line<T, 64, 8, F2, ROWS, FUSE, true>, 64);
+				if (fv.pf)
+					go(k_md_line<T, 128, 4, F2, ROWS, FUSE, true, false, true>, 128);
 				else
 					go(k_md_line<T, 128, 4, F2, ROWS, FUSE, true>, 128);
+				return;
+			}
+			if (fv.pf)
+			{
+				go(k_md_line<T, 128, 4, F2, ROWS, FUSE, false, false, true>, 128);
 				return;
 			}
 		}

@@ -284,6 +284,25 @@ template <bool ROWS, bool R2> struct LineLoad<float, ROWS, R2>
 		else
 			return (*this)(mu, s);
 	}
+	// L1 prefetch of what rows() / operator() will read (one 128-byte line
+	// per plane of the warp's addresses)
+	__device__ __forceinline__ static void pf(void const *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+	__device__ __forceinline__ void prefetch_rows(int mu, uint32_t s) const
+	{
+		float4 const *p = reinterpret_cast<float4 const *>(U) + (uint32_t(mu) * 9u * (V >> 1) + s);
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			pf(p + k * V);
+	}
+	__device__ __forceinline__ void prefetch(int mu, uint32_t s) const
+	{
+		prefetch_rows(mu, s);
+		if constexpr (!(ROWS && !R2))
+		{
+			pf(reinterpret_cast<float4 const *>(U) + (uint32_t(mu) * 9u * (V >> 1) + 3 * V + s));
+			pf(reinterpret_cast<float2 const *>(U) + (uint32_t(mu) * 9u * V + 8 * V + s));
+		}
+	}
 };
 template <bool ROWS, bool R2> struct LineLoad<double, ROWS, R2>
 {
@@ -315,6 +334,8 @@ template <bool ROWS, bool R2> struct LineLoad<double, ROWS, R2>
 		planes<6>(mu, s, e);
 		return e;
 	}
+	__device__ __forceinline__ void prefetch_rows(int, uint32_t) const {}
+	__device__ __forceinline__ void prefetch(int, uint32_t) const {}
 };
 
 // site coordinates of the line march (x3 of the lane, x2 of its sub-line)
@@ -569,7 +590,8 @@ __device__ __forceinline__ void line_carry(Geom const &g, LineSite const &x, LD 
 
 // One momentum step (and with FUSE the link update after it) of every link,
 // line-marching. P -= coef F(U); Uout = exp(tu P) U (reunitised when reunit).
-template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE, bool R2 = false, bool FSM = false>
+template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE, bool R2 = false, bool FSM = false,
+          bool PF = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_md_line(Geom g, LineSpec ls, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
               T *__restrict__ Uout, T tu, int reunit)
@@ -631,6 +653,23 @@ __global__ void __launch_bounds__(NT, MINB)
 		for (int q = 0; q < 6; ++q)
 		{
 			int mu = plane_mu<4>(q), nu = plane_nu<4>(q);
+			if constexpr (PF)
+			{
+				// the neighbour links of the next plane (or, after the last
+				// plane, of the first lower staple) into L1 while this one runs
+				if (q < 5)
+				{
+					int m2 = plane_mu<4>(q + 1), n2 = plane_nu<4>(q + 1);
+					ld.prefetch(n2, nb.fwd(m2));
+					ld.prefetch(m2, nb.fwd(n2));
+				}
+				else
+				{
+					ld.prefetch_rows(0, nb.b2);
+					ld.prefetch(2, nb.diag(2, 0));
+					ld.prefetch(2, nb.b2);
+				}
+			}
 			T o[8];
 			plaquette_at<T, F2>(s, nb.fwd(mu), nb.fwd(nu), mu, nu, ld, o);
 			F.add(mu, o, T(1));
@@ -667,6 +706,19 @@ __global__ void __launch_bounds__(NT, MINB)
 				if (nu == mu)
 					continue;
 				uint32_t y = nu == 0 ? nb.b0 : nb.b2;
+				if constexpr (PF)
+				{
+					// the next lower staple's links: (mu, 2) after (mu, 0); else
+					// the next link's first staple
+					int mn = r == 0 && mu != 2 ? mu : mu + 1, nn = r == 0 && mu != 2 ? 2 : (mu + 1 == 0 ? 2 : 0);
+					if (mn < 4)
+					{
+						uint32_t yn = nn == 0 ? nb.b0 : nb.b2;
+						ld.prefetch_rows(mn, yn);
+						ld.prefetch(nn, nb.diag(nn, mn));
+						ld.prefetch(nn, yn);
+					}
+				}
 				E f = ld(nu, nb.diag(nu, mu));
 				E ef = PrO::mul_r2(ld.rows(mu, y), f);
 				Gp::add_to(S, PrO::mul_dn(ef, ld(nu, y)));
