@@ -709,6 +709,69 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 		}
 }
 
+// Force accumulators F[mu][a] of the thread-per-site body: in registers, or
+// (SM) in a block of shared memory private to the thread, element (mu, a) at
+// sm[(mu NA + a) 32] past the thread's lane (a warp's 32 threads touch 32
+// consecutive words: no bank conflicts). Shared memory frees the ND x NA
+// registers for a higher occupancy at the cost of a load and a store per
+// accumulated real.
+template <class T, int ND, int NA, bool SM> struct SiteAcc;
+template <class T, int ND, int NA> struct SiteAcc<T, ND, NA, false>
+{
+	T F[ND][NA];
+	__device__ __forceinline__ explicit SiteAcc(T *)
+	{
+#pragma unroll
+		for (int mu = 0; mu < ND; ++mu)
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				F[mu][a] = T(0);
+	}
+	__device__ __forceinline__ void plane(int q, T const *x) { add_plane<ND, NA>(F, q, x); }
+	__device__ __forceinline__ void dir(int mu, T const *x) { add_dir<ND, NA>(F, mu, x); }
+	__device__ __forceinline__ void get(int mu, T *f) const
+	{
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+		{
+			f[a] = F[0][a];
+#pragma unroll
+			for (int k = 1; k < ND; ++k)
+				f[a] = mu == k ? F[k][a] : f[a];
+		}
+	}
+};
+template <class T, int ND, int NA> struct SiteAcc<T, ND, NA, true>
+{
+	T *sm; // the thread's first element: warp block + lane
+	__device__ __forceinline__ explicit SiteAcc(T *p) : sm(p)
+	{
+#pragma unroll
+		for (int k = 0; k < ND * NA; ++k)
+			sm[32 * k] = T(0);
+	}
+	__device__ __forceinline__ void add(int mu, T const *x, T sg)
+	{
+		T *b = sm + 32 * NA * mu;
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			b[32 * a] += sg * x[a];
+	}
+	__device__ __forceinline__ void plane(int q, T const *x)
+	{
+		add(plane_mu<ND>(q), x, T(1));
+		add(plane_nu<ND>(q), x, T(-1));
+	}
+	__device__ __forceinline__ void dir(int mu, T const *x) { add(mu, x, T(1)); }
+	__device__ __forceinline__ void get(int mu, T *f) const
+	{
+		T const *b = sm + 32 * NA * mu;
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			f[a] = b[32 * a];
+	}
+};
+
 // Momentum step, one thread per site updating the momenta of all ND links of
 // the site. With a = U_mu(x), b = U_nu(x+mu), c = U_mu(x+nu), d = U_nu(x),
 // the forward staple of link (x, mu) in the plane (mu, nu) closes to the
@@ -732,22 +795,17 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 // momenta when want_kin (the FP64 sum costs FP64-pipe time: only the last
 // momentum step of a trajectory asks for it). Shared by k_momentum_step_site
 // and the batched replicas.
-template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD>
+template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD, bool SM = false>
 __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld,
                                           T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
-                                          bool want_kin)
+                                          bool want_kin, T *acc_sm = nullptr)
 {
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	using Pr = Prod<GRP, T, F2>;
 	constexpr int NA = Gp::NA;
 	double acc = 0.0;
-	T F[ND][NA];
-#pragma unroll
-	for (int mu = 0; mu < ND; ++mu)
-#pragma unroll
-		for (int a = 0; a < NA; ++a)
-			F[mu][a] = T(0);
+	SiteAcc<T, ND, NA, SM> F(acc_sm);
 	// forward plaquette loops, one per plane
 #pragma unroll 1
 	for (int q = 0; q < ND * (ND - 1) / 2; ++q)
@@ -768,7 +826,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		E pl = Pr::mul_nd(ab, dc);
 		T xa[NA];
 		Gp::proj(pl, xa);
-		add_plane<ND, NA>(F, q, xa);
+		F.plane(q, xa);
 	}
 	// backward staples
 #pragma unroll 1
@@ -792,7 +850,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		E W = Pr::mul(ld(mu, s), S);
 		T xa[NA];
 		Gp::proj(W, xa);
-		add_dir<ND, NA>(F, mu, xa);
+		F.dir(mu, xa);
 	}
 	if constexpr (!FUSE)
 	{
@@ -800,11 +858,12 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		for (int mu = 0; mu < ND; ++mu)
 		{
 			auto Pv = comp<T, NA>(P, g.V, mu);
-			T p[NA];
+			T p[NA], f[NA];
+			F.get(mu, f);
 			Pv.template load<CACHE_STREAM>(s, p);
 #pragma unroll
 			for (int a = 0; a < NA; ++a)
-				p[a] -= coef * F[mu][a];
+				p[a] -= coef * f[a];
 			Pv.template store<CACHE_STREAM>(s, p);
 			if (want_kin)
 				acc += double(Gp::kin(p));
@@ -817,14 +876,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		for (int mu = 0; mu < ND; ++mu)
 		{
 			T f[NA];
-#pragma unroll
-			for (int a = 0; a < NA; ++a)
-			{
-				f[a] = F[0][a];
-#pragma unroll
-				for (int k = 1; k < ND; ++k)
-					f[a] = mu == k ? F[k][a] : f[a];
-			}
+			F.get(mu, f);
 			auto Pv = comp<T, NA>(P, g.V, mu);
 			T p[NA];
 			Pv.template load<CACHE_STREAM>(s, p);
@@ -847,12 +899,17 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	return acc;
 }
 
-template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false>
+template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false,
+          bool SM = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
 {
 	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
+	constexpr int NA = Group<GRP, T>::NA;
+	// SM: the threads' force accumulators, [warp][element][lane]
+	__shared__ T sm_acc[SM ? NT * ND * NA : 1];
+	T *my = SM ? sm_acc + (threadIdx.x >> 5) * (32 * ND * NA) + (threadIdx.x & 31) : nullptr;
 	double acc = 0.0;
 	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
 	{
@@ -862,7 +919,8 @@ __global__ void __launch_bounds__(NT, MINB)
 			tile_site<ND>(ts, tile, t, x);
 			Site<ND> st = site_from_coords<ND>(g, x);
 			int64_t s = eo_of<ND>(g, st);
-			acc += site_md<GRP, T, ND, F2, ROWS, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit, kin.result != nullptr);
+			acc += site_md<GRP, T, ND, F2, ROWS, FUSE, decltype(ld), SM>(g, st, s, ld, P, coef, Uout, tu, reunit,
+			                                                            kin.result != nullptr, my);
 		}
 	}
 	if (kin.result)
@@ -1589,6 +1647,7 @@ template <int GRP, class T, int ND> struct Ops
 		int r2 = 0;        // line march: row 2 of whole-link loads read, not rebuilt
 		int fsm = 0;       // line march: force accumulators in shared memory
 		int pf = 0;        // line march: L1 prefetch of the next iteration's links
+		int sm = 0;        // thread per site: force accumulators in shared memory
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1597,8 +1656,9 @@ template <int GRP, class T, int ND> struct Ops
 	// 18-20: thread per site, plain products (every group and precision);
 	// 29-34: SU(3) line march (k_md_line: plaquettes computed once, lower
 	// staples along x1 and x3 handed over), launch shapes, products and
-	// whether row 2 of whole links is read or rebuilt
-	static constexpr int kForceVariants = 35;
+	// whether row 2 of whole links is read or rebuilt; 35-36: thread per site
+	// with the force accumulators in shared memory (five blocks per SM)
+	static constexpr int kForceVariants = 37;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1637,7 +1697,9 @@ template <int GRP, class T, int ND> struct Ops
 		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/fsm/pf", 1, 0, 1, 1},
 		    {3, {0, 0, 0, 0}, 128, 5, "line/128thr/5blk/f32x2/fsm", 1, 0, 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2", 1, 1},
-		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2/pf", 1, 1, 0, 1}};
+		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2/pf", 1, 1, 0, 1},
+		    {2, {1, 1, 2, 3}, 128, 5, "site/tile2x2x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1},
+		    {2, {0, 2, 2, 3}, 128, 5, "site/tile1x4x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1740,6 +1802,15 @@ template <int GRP, class T, int ND> struct Ops
 	static void site_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u, T *p,
 	                     T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
 	{
+		if constexpr (GRP == SU3 && ROWS && F2)
+		{
+			if (fv.sm)
+			{
+				k_momentum_step_site<GRP, T, 4, 128, 5, F2, ROWS, FUSE, true>
+				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				return;
+			}
+		}
 		if (fv.threads == 512)
 			k_momentum_step_site<GRP, T, 4, 512, 1, F2, ROWS, FUSE>
 			    <<<b, 512, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
@@ -1841,7 +1912,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 34; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 36; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)

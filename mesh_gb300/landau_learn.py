@@ -276,7 +276,9 @@ def main():
                     help="acceptance test of the Fourier-accelerated steps (survey, train, compare)")
     ap.add_argument("--alphas", default=None, help="train: comma-separated step sizes of the family search")
     ap.add_argument("--highs", default=None, help="train: comma-separated high-mode factors of the family search")
-    ap.add_argument("--fixed", default="0.08,0.35", help="compare: the fixed family member alpha,high")
+    ap.add_argument("--fixed", default="0.08,0.6", help="compare: the fixed family member alpha,high")
+    ap.add_argument("--weights", default=WEIGHTS, help="compare: the network to evaluate")
+    ap.add_argument("--methods", default="or,plain,fixed,learned", help="compare: solvers to run")
     args = ap.parse_args()
     ctx = Context(0)
     if args.mode == "survey":
@@ -322,29 +324,31 @@ def main():
                           "first_loss": float(losses[0]), "target_variance": float(np.var(data[:, 3])),
                           "t_generate_and_collect_s": t_collect, "configs": ncfg}))
     else:
-        params, gamma = load_weights()
+        params, gamma = load_weights(args.weights)
         seeds = np.arange(1, args.eval_configs + 1)
         cfgs = hmc_configs(ctx, args.eval_L, [6.0] * len(seeds), seeds, args.eval_therm, 1, 0)
         rows = []
         fixed = tuple(float(x) for x in args.fixed.split(","))
-        methods = ("or", "plain", "fixed", "learned")
+        methods = tuple(m for m in args.methods.split(",") if m)
         for k, (beta, Uh) in enumerate(cfgs):
             for method in methods:
                 U = prepared_links(ctx, Uh, transform_seed=5)
                 r = solve(ctx, U, method, params, beta, accept=args.accept, member=fixed)
                 r["config"] = k
+                r["cost"] = r["iterations"] + 11 * r["fallbacks"] if method != "or" else r["iterations"]
                 rows.append(r)
                 print(json.dumps(r), flush=True)
-        summ = {"accept": args.accept, "fixed_member": fixed}
+        summ = {"accept": args.accept, "fixed_member": fixed, "weights": os.path.basename(args.weights)}
         for m in methods:
             rs = [r for r in rows if r["method"] == m]
             summ[m] = {"mean_seconds": float(np.mean([r["seconds"] for r in rs])),
                        "mean_iterations": float(np.mean([r["iterations"] for r in rs])),
                        "total_fallbacks": int(sum(r["fallbacks"] for r in rs)),
+                       "total_cost": int(sum(r["cost"] for r in rs)),
                        "max_theta": float(max(r["theta"] for r in rs))}
-        summ["speedup_learned_vs_or"] = summ["or"]["mean_seconds"] / summ["learned"]["mean_seconds"]
-        summ["speedup_learned_vs_plain"] = summ["plain"]["mean_seconds"] / summ["learned"]["mean_seconds"]
-        summ["speedup_learned_vs_fixed"] = summ["fixed"]["mean_seconds"] / summ["learned"]["mean_seconds"]
+        for m in ("or", "plain", "fixed"):
+            if m in summ and "learned" in summ:
+                summ[f"speedup_learned_vs_{m}"] = summ[m]["mean_seconds"] / summ["learned"]["mean_seconds"]
         print(json.dumps(summ))
         if args.json:
             with open(args.json, "w") as fh:
