@@ -44,7 +44,7 @@ extern "C" {
 #define MESH_ERR_ARG 1         /* invalid argument (shape, group, size, kind) */
 #define MESH_ERR_CUDA 2        /* CUDA runtime error (device.cpp:11-18 analogue) */
 #define MESH_ERR_STATE 3       /* objects on different grids/contexts, wrong state */
-/* 4 is not used: no kernel of this library waits on another block or a flag */
+#define MESH_ERR_TIMEOUT 4     /* a bounded device-side wait expired (the launch's results are invalid) */
 #define MESH_ERR_NUMERIC 5     /* NaN/Inf in an action, Hamiltonian or theta */
 #define MESH_ERR_NOCONV 6      /* iteration limit reached without convergence */
 #define MESH_ERR_UNSUPPORTED 7 /* valid request this build does not implement */

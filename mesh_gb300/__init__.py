@@ -37,7 +37,7 @@ NALG = {U1: 1, SU2: 3, SU3: 8}
 NC = {U1: 1, SU2: 2, SU3: 3}
 
 STATUS = {
-    0: "MESH_OK", 1: "MESH_ERR_ARG", 2: "MESH_ERR_CUDA", 3: "MESH_ERR_STATE",
+    0: "MESH_OK", 1: "MESH_ERR_ARG", 2: "MESH_ERR_CUDA", 3: "MESH_ERR_STATE", 4: "MESH_ERR_TIMEOUT",
     5: "MESH_ERR_NUMERIC", 6: "MESH_ERR_NOCONV", 7: "MESH_ERR_UNSUPPORTED",
 }
 

@@ -13,6 +13,21 @@
 
 using namespace meshgb;
 
+// the context's device error word (bounded device-side waits): reads it
+// (synchronising the stream), clears it and reports a nonzero code
+void meshgb::check_device_error(Context &c)
+{
+	int e = 0;
+	MESH_CUDA(cudaMemcpyAsync(&e, c.d_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+	MESH_CUDA(cudaStreamSynchronize(c.stream));
+	if (e)
+	{
+		MESH_CUDA(cudaMemsetAsync(c.d_err, 0, sizeof(int), c.stream));
+		throw Error(MESH_ERR_TIMEOUT, "a bounded device-side wait expired (TMA copy of a lattice line did not "
+		                              "complete); the launch's results are invalid");
+	}
+}
+
 namespace {
 void teardown_ctx(Context &c)
 {
@@ -22,6 +37,7 @@ void teardown_ctx(Context &c)
 	cudaFree(c.d_partials);
 	cudaFree(c.d_results);
 	cudaFree(c.d_counters);
+	cudaFree(c.d_err);
 	if (c.d_stage)
 		cudaFree(c.d_stage);
 	if (c.own_stream && c.stream)
@@ -367,6 +383,7 @@ struct mesh_hmc_s
 
 	void check_bad()
 	{
+		check_device_error(*ctx);
 		int bad = 0;
 		MESH_CUDA(cudaMemcpyAsync(&bad, &d_dev->bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
 		MESH_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -411,6 +428,8 @@ int mesh_ctx_create(int device, void *stream, mesh_ctx *out)
 		MESH_CUDA(cudaMalloc(&c.d_counters, sizeof(unsigned) * kSlots));
 		MESH_CUDA(cudaMemset(c.d_counters, 0, sizeof(unsigned) * kSlots));
 		MESH_CUDA(cudaMemset(c.d_results, 0, sizeof(double) * kSlots));
+		MESH_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
+		MESH_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
 	});
 	if (rc != MESH_OK)
 	{
@@ -435,6 +454,7 @@ int mesh_ctx_synchronize(mesh_ctx h)
 	return api([&] {
 		require(h != nullptr, "null context");
 		MESH_CUDA(cudaStreamSynchronize(h->c.stream));
+		check_device_error(h->c);
 	});
 }
 

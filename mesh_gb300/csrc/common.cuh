@@ -56,6 +56,9 @@ struct Context
 	double *d_partials = nullptr;
 	double *d_results = nullptr;
 	unsigned *d_counters = nullptr;
+	// device error word: kernels with bounded waits (the TMA-staged line march)
+	// write a nonzero code here when a wait gives up; zero otherwise
+	int *d_err = nullptr;
 	// host staging for layout conversions
 	void *d_stage = nullptr;
 	size_t stage_bytes = 0;

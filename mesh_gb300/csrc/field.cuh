@@ -161,6 +161,10 @@ inline OpsTable const &ops_for(Field const &f) { return ops_for(f.group, f.prec,
 // MLP inference on device arrays (mlp.cu): y[n] = MLP(x[n][3])
 void mlp_forward_device(Context &c, int n, float const *d_x, float const *d_params, int width, bool bf16, float *d_y);
 
+// throws MESH_ERR_TIMEOUT when a kernel of the context gave up a bounded
+// device-side wait (capi.cu)
+void check_device_error(Context &c);
+
 // the error message reported by mesh_last_error() (capi.cu)
 void set_last_error(char const *msg);
 

@@ -1648,6 +1648,7 @@ template <int GRP, class T, int ND> struct Ops
 		int fsm = 0;       // line march: force accumulators in shared memory
 		int pf = 0;        // line march: L1 prefetch of the next iteration's links
 		int sm = 0;        // thread per site: force accumulators in shared memory
+		int st = 0;        // line march: own line staged in shared memory by bulk copies (L3 = 32)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1657,8 +1658,9 @@ template <int GRP, class T, int ND> struct Ops
 	// 29-34: SU(3) line march (k_md_line: plaquettes computed once, lower
 	// staples along x1 and x3 handed over), launch shapes, products and
 	// whether row 2 of whole links is read or rebuilt; 35-36: thread per site
-	// with the force accumulators in shared memory (five blocks per SM)
-	static constexpr int kForceVariants = 37;
+	// with the force accumulators in shared memory (five blocks per SM); 37:
+	// line march with the warp's own line staged by bulk copies (TMA)
+	static constexpr int kForceVariants = 38;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1699,7 +1701,8 @@ template <int GRP, class T, int ND> struct Ops
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2", 1, 1},
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2/pf", 1, 1, 0, 1},
 		    {2, {1, 1, 2, 3}, 128, 5, "site/tile2x2x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1},
-		    {2, {0, 2, 2, 3}, 128, 5, "site/tile1x4x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1}};
+		    {2, {0, 2, 2, 3}, 128, 5, "site/tile1x4x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1},
+		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/tma", 1, 0, 0, 0, 0, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1712,7 +1715,7 @@ template <int GRP, class T, int ND> struct Ops
 		if (!fv.tiled)
 			return true;
 		if (fv.tiled == 3)
-			return GRP == SU3 && ND == 4 && line_supported(g);
+			return GRP == SU3 && ND == 4 && line_supported(g) && (!fv.st || (kF2 && g.L[3] == 32));
 		if (ND != 4)
 			return false;
 		for (int i = 0; i < 4; ++i)
@@ -1844,6 +1847,7 @@ template <int GRP, class T, int ND> struct Ops
 			int64_t nseg = resident / ls.ncol;
 			ls.nseg = int(nseg < 1 ? 1 : (nseg > g.L[1] ? g.L[1] : nseg));
 			ls.nwork = ls.ncol * ls.nseg;
+			ls.err = c.d_err;
 			unsigned b = unsigned((ls.nwork + wpb - 1) / wpb);
 			if constexpr (sizeof(T) == 8)
 				k_md_line<T, 64, 6, 0, ROWS, FUSE><<<b, 64, 0, c.stream>>>(g, ls, u, p, coef, kin, uo, tu, reunit);
@@ -1865,6 +1869,11 @@ template <int GRP, class T, int ND> struct Ops
 		};
 		if constexpr (ROWS && F2)
 		{
+			if (fv.st)
+			{
+				go(k_md_line<T, 64, 8, F2, ROWS, FUSE, false, false, false, true>, 64);
+				return;
+			}
 			if (fv.fsm)
 			{
 				if (fv.pf)
@@ -1912,7 +1921,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 36; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 37; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)

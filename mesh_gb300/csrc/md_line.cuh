@@ -52,6 +52,7 @@ struct LineSpec
 	int ncol; // columns of lines along x1: L0 * L2 / ns
 	int nseg; // segments of the x1 march per column
 	int nwork; // warps with work: ncol * nseg
+	int *err;  // the context's device error word (bounded waits of the staged variant)
 };
 
 inline bool line_supported(Geom const &g)
@@ -590,8 +591,62 @@ __device__ __forceinline__ void line_carry(Geom const &g, LineSite const &x, LD 
 
 // One momentum step (and with FUSE the link update after it) of every link,
 // line-marching. P -= coef F(U); Uout = exp(tu P) U (reunitised when reunit).
+// ---- bulk copies (TMA) into shared memory with an mbarrier ------------------
+// One warp stages its own line (rows 0, 1 of the four links: per link 3
+// float4 planes x 2 parities, each a contiguous 256-byte run of the even/odd
+// layout when L3 = 32) with 24 cp.async.bulk copies issued by lane 0, which
+// complete on the warp's mbarrier. Every wait is bounded in time; a wait that
+// gives up writes a code to the context's device error word and the warp
+// stops working (the host reports MESH_ERR_TIMEOUT).
+__device__ __forceinline__ uint32_t smem_addr(void const *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(unsigned long long *b)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(b)) : "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect(unsigned long long *b, uint32_t bytes)
+{
+	asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+	                 smem_addr(b)),
+	             "r"(bytes)
+	             : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void *dst, void const *src, uint32_t bytes, unsigned long long *b)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 smem_addr(dst)),
+	             "l"(src), "r"(bytes), "r"(smem_addr(b))
+	             : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long *b, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, "
+	             "p;\n\t}"
+	             : "=r"(ok)
+	             : "r"(smem_addr(b)), "r"(parity)
+	             : "memory");
+	return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns()
+{
+	uint64_t t;
+	asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+	return t;
+}
+// waits for the phase `parity` of b for at most `limit_ns`; false on timeout
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *b, uint32_t parity, uint64_t limit_ns)
+{
+	uint64_t t0 = global_ns();
+	while (!mbar_try(b, parity))
+		if (global_ns() - t0 > limit_ns)
+			return false;
+	return true;
+}
+constexpr uint64_t kWaitLimitNs = 200000000ull; // 0.2 s: a line copy takes microseconds
+
 template <class T, int NT, int MINB, int F2, bool ROWS, bool FUSE, bool R2 = false, bool FSM = false,
-          bool PF = false>
+          bool PF = false, bool ST = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_md_line(Geom g, LineSpec ls, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
               T *__restrict__ Uout, T tu, int reunit)
@@ -609,6 +664,11 @@ __global__ void __launch_bounds__(NT, MINB)
 	__shared__ SW sm_x1[NW][NS];
 	// FSM: the force accumulators of the warp's threads, [link][word][lane]
 	__shared__ SW sm_f[FSM ? NW : 1][FSM ? 4 * Slot16<T>::N * 32 : 1];
+	// ST (float, L3 = 32): the warp's own line, rows 0, 1 of the four links,
+	// [link][plane][parity][x3 / 2] float4, filled by bulk copies
+	static_assert(!ST || (sizeof(T) == 4 && ROWS), "staged lines: FP32 links read as rows 0, 1");
+	__shared__ __align__(128) float4 sm_own[ST ? NW : 1][ST ? 24 * 16 : 1];
+	__shared__ __align__(8) unsigned long long sm_bar[ST ? NW : 1];
 	LineLoad<T, ROWS, R2> ld{U, uint32_t(g.V)};
 	int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	SW *s3 = sm_x3[wib];
@@ -621,7 +681,43 @@ __global__ void __launch_bounds__(NT, MINB)
 	int col = wid % ls.ncol, seg = wid / ls.ncol;
 	int t0 = seg * L1 / ls.nseg, t1 = wid < ls.nwork ? (seg + 1) * L1 / ls.nseg : t0;
 	double acc = 0.0;
-	for (int t = t0; t < t1; ++t)
+	// ST: copy the line (x0, t, x2) of every link's rows 0, 1 into sm_own
+	float4 *own = ST ? sm_own[wib] : nullptr;
+	unsigned long long *bar = ST ? &sm_bar[wib] : nullptr;
+	uint32_t phase = 0;
+	bool bad = false;
+	auto stage = [&](int t) {
+		if constexpr (ST)
+		{
+			if (lane == 0)
+			{
+				int x0 = col / ngrp, x2 = col - x0 * ngrp;
+				uint32_t lbh = uint32_t((x0 * L1 + t) * g.L[2] + x2) * 16u;
+				uint32_t V = uint32_t(g.V), Vh = uint32_t(g.Vh);
+				float4 const *U4 = reinterpret_cast<float4 const *>(U);
+				// the generic-proxy reads of the previous line come before the
+				// copies overwrite it
+				asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+				mbar_expect(bar, 24u * 256u);
+#pragma unroll 1
+				for (int c = 0; c < 24; ++c)
+				{
+					int mu = c / 6, k = (c / 2) % 3, p = c & 1;
+					bulk_to_smem(own + c * 16, U4 + (uint32_t(mu) * 9u * (V >> 1) + uint32_t(k) * V + p * Vh + lbh),
+					             256u, bar);
+				}
+			}
+		}
+	};
+	if constexpr (ST)
+	{
+		if (lane == 0)
+			mbar_init(bar);
+		__syncwarp();
+		if (t0 < t1)
+			stage(t0);
+	}
+	for (int t = t0; t < t1 && !bad; ++t)
 	{
 		LineSite x;
 		x.x1 = t;
@@ -629,6 +725,44 @@ __global__ void __launch_bounds__(NT, MINB)
 		x.x2 = (col - x.x0 * ngrp) * ls.ns + sub;
 		x.x3 = lane % L3;
 		uint32_t s = line_eo(g, x.x0, x.x1, x.x2, x.x3);
+		if constexpr (ST)
+		{
+			// the line's copies (issued at the end of the previous step)
+			// a warp-uniform decision: all lanes leave together or none
+			bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bar, phase, kWaitLimitNs));
+			if (!ok)
+			{
+				if (lane == 0 && ls.err)
+					atomicExch(ls.err, 1);
+				bad = true;
+				break;
+			}
+			phase ^= 1u;
+		}
+		// own links from the staged line: lane xl of the warp's line, rows 0, 1
+		auto own_rows = [&](int mu, int xl) {
+			E e;
+			if constexpr (ST)
+			{
+				int pl = (x.x0 + x.x1 + x.x2 + xl) & 1;
+#pragma unroll
+				for (int k = 0; k < 3; ++k)
+				{
+					float4 w = own[((mu * 3 + k) * 2 + pl) * 16 + (xl >> 1)];
+					e.v[4 * k] = w.x;
+					e.v[4 * k + 1] = w.y;
+					e.v[4 * k + 2] = w.z;
+					e.v[4 * k + 3] = w.w;
+				}
+			}
+			return e;
+		};
+		auto own_full = [&](int mu, int xl) {
+			E e = own_rows(mu, xl);
+			Gp::complete_row2(e);
+			return e;
+		};
+		int lane_next = (lane + 1) & 31;
 		if (t == t0)
 			line_carry<T, F2>(g, x, ld, s1, lane);
 		LineNb nb = line_neighbours(g, x);
@@ -671,7 +805,16 @@ __global__ void __launch_bounds__(NT, MINB)
 				}
 			}
 			T o[8];
-			plaquette_at<T, F2>(s, nb.fwd(mu), nb.fwd(nu), mu, nu, ld, o);
+			if constexpr (ST)
+			{
+				// rows of U_mu(x), U_nu(x) and U_mu(x + e_3) from the staged line
+				E M1 = Pr::mul01(own_rows(mu, lane), ld(nu, nb.fwd(mu)));
+				E M2 = Pr::mul01(own_rows(nu, lane), nu == 3 ? own_full(mu, lane_next) : ld(mu, nb.fwd(nu)));
+				Gp::complete_row2(M2);
+				Pr::proj01(Pr::mul01_nd(M1, M2), o);
+			}
+			else
+				plaquette_at<T, F2>(s, nb.fwd(mu), nb.fwd(nu), mu, nu, ld, o);
 			F.add(mu, o, T(1));
 			F.add(nu, o, T(-1));
 			// hand-overs: along x1 (planes with mu or nu = 1), along x3 (nu = 3)
@@ -687,7 +830,7 @@ __global__ void __launch_bounds__(NT, MINB)
 				int k = dir == nu ? mu : nu;
 				T sg = dir == nu ? T(-1) : T(1);
 				T c[8];
-				Pr::adjoint(ld(dir, s), o, sg, c);
+				Pr::adjoint(ST ? own_full(dir, lane) : ld(dir, s), o, sg, c);
 				if (r == 0)
 					slot_store<T>(s1, k == 0 ? 0 : k - 1, lane, c);
 				else
@@ -724,7 +867,7 @@ __global__ void __launch_bounds__(NT, MINB)
 				Gp::add_to(S, PrO::mul_dn(ef, ld(nu, y)));
 			}
 			T xa[NA];
-			Pr::proj_mul(ld(mu, s), S, xa);
+			Pr::proj_mul(ST ? own_full(mu, lane) : ld(mu, s), S, xa);
 			F.add(mu, xa, T(1));
 		}
 		// contributions from x - e_3 (the previous lane): links 0, 1, 2
@@ -758,7 +901,7 @@ __global__ void __launch_bounds__(NT, MINB)
 			{
 				E r;
 				if constexpr (ROWS)
-					r = PrO::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
+					r = PrO::mul_r2(Gp::exp_alg(p, tu), ST ? own_full(mu, lane) : ld(mu, s));
 				else
 					r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
 				if (reunit)
@@ -766,6 +909,20 @@ __global__ void __launch_bounds__(NT, MINB)
 				comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
 			}
 		}
+		if constexpr (ST)
+		{
+			// every lane is done with this line: copy the next one
+			__syncwarp();
+			if (t + 1 < t1)
+				stage(t + 1);
+		}
+	}
+	if constexpr (ST)
+	{
+		// after a wait gave up, the copies still in flight land before the
+		// block's shared memory is released (bounded as well)
+		if (bad)
+			mbar_wait_bounded(bar, phase, kWaitLimitNs);
 	}
 	if (kin.result)
 		grid_sum<NT>(acc, kin);

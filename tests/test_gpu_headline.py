@@ -15,7 +15,7 @@ import mesh_gb300 as mg
 
 pytestmark = pytest.mark.gpu
 
-LINE_VARIANTS = (29, 30, 31, 32, 33, 34)
+LINE_VARIANTS = (29, 30, 31, 32, 33, 34, 37)
 
 
 def rel(a, b):
