@@ -66,7 +66,10 @@ def parse():
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
     ap.add_argument("--fa-accept", choices=["theta", "functional"], default="theta",
                     help="landau workload: acceptance test of the Fourier-accelerated steps")
-    ap.add_argument("--methods", default="or,plain,learned", help="landau workload: solvers to run")
+    ap.add_argument("--methods", default="or,plain,learned",
+                    help="landau workload: solvers to run (or, plain, fixed, learned)")
+    ap.add_argument("--fixed", default="0.08,0.6", help="landau workload: the fixed multiplier member alpha,high")
+    ap.add_argument("--weights", default=None, help="landau workload: network file (default: the committed one)")
     ap.add_argument("--fp64", action="store_true",
                     help="hmc workload: the plain all-FP64 chain (links, momenta, force in FP64) instead of the "
                          "mixed-precision one, for the FP64-vs-mixed comparison")
@@ -733,16 +736,20 @@ def run_landau(args):
     L = args.lattice
     seeds = np.arange(1, args.configs + 1)
     cfgs = ll.hmc_configs(ctx, L, [6.0] * len(seeds), seeds, args.therm, 1, 0)
-    params, _ = ll.load_weights()
+    params, _ = ll.load_weights(args.weights) if args.weights else ll.load_weights()
+    fixed = tuple(float(x) for x in args.fixed.split(","))
     methods = [m for m in args.methods.split(",") if m]
     rows = []
     for k, (beta, Uh) in enumerate(cfgs):
         for method in methods:
             U = ll.prepared_links(ctx, Uh, transform_seed=5)
-            r = ll.solve(ctx, U, method, params, beta, accept=args.fa_accept)
+            r = ll.solve(ctx, U, method, params, beta, accept=args.fa_accept, member=fixed)
             r["config"] = k
+            r["seed"] = int(seeds[k])
             r["cost"] = r["iterations"] + 11 * r["fallbacks"]
             rows.append(r)
+            print(json.dumps({"row": r}), flush=True)
+            U.close()
     summ = {m: {"mean_seconds": float(np.mean([r["seconds"] for r in rows if r["method"] == m])),
                 "mean_iterations": float(np.mean([r["iterations"] for r in rows if r["method"] == m])),
                 "fallbacks": int(sum(r["fallbacks"] for r in rows if r["method"] == m)),
@@ -756,9 +763,9 @@ def run_landau(args):
                                            "thermalisation": f"{args.therm} trajectories, seeds 1..{len(seeds)}",
                                            "transform": "Haar-random, seed 5", "fa_accept": args.fa_accept,
                                            "cost": "descent steps + 11 per overrelaxation fallback"},
-           "summary": summ, "rows": rows}
+           "summary": summ, "rows": rows, "fixed_member": fixed}
     if "or" in summ:
-        for m in ("learned", "plain"):
+        for m in ("learned", "plain", "fixed"):
             if m in summ:
                 out[f"speedup_{m}_vs_or"] = summ["or"]["mean_seconds"] / summ[m]["mean_seconds"]
     print(json.dumps(out), flush=True)
