@@ -64,7 +64,7 @@ def parse():
                          "configuration; heatbath: heat-bath + overrelaxation sweeps; fp64-8x4: the FP64 8^4 "
                          "cold-start chain against the CPU oracle, trajectory by trajectory")
     ap.add_argument("--configs", type=int, default=2, help="landau workload: number of configurations")
-    ap.add_argument("--fa-accept", choices=["theta", "functional"], default="theta",
+    ap.add_argument("--fa-accept", choices=["theta", "functional"], default="functional",
                     help="landau workload: acceptance test of the Fourier-accelerated steps")
     ap.add_argument("--methods", default="or,plain,learned",
                     help="landau workload: solvers to run (or, plain, fixed, learned)")
@@ -279,8 +279,9 @@ def landau_one_config(ctx, L=24, therm=100):
     """Landau gauge fixing of one thermalised SU(3) L^4 beta = 6.0
     configuration (HMC seed 1, Haar-random transform seed 5) to
     theta < 1e-12: FP64 overrelaxation (omega 1.7), Fourier acceleration with
-    the plain and with the learned multiplier (steps accepted on theta,
-    overrelaxation fallback): seconds, iterations, fallbacks, functional."""
+    the plain and with the learned multiplier (steps accepted on the gauge
+    functional, overrelaxation fallback): seconds, iterations, fallbacks,
+    functional."""
     from mesh_gb300 import landau_learn as ll
 
     (beta, Uh), = list(ll.hmc_configs(ctx, L, [6.0], [1], therm, 1, 0))

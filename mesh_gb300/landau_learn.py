@@ -212,7 +212,7 @@ def train(ctx, data, epochs=200, batch=1024, lr=2e-3, seed=0):
     return params, losses
 
 
-def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omega=1.7, accept="theta",
+def solve(ctx, U, method, params=None, beta=6.0, tol=1e-12, max_iter=20000, omega=1.7, accept="functional",
           member=None):
     """Fix U to Landau gauge from g = 1 with `method` in {"or", "plain",
     "learned", "fixed"} ("fixed": the family member (alpha, high) given as
@@ -272,7 +272,7 @@ def main():
     ap.add_argument("--json", default=None)
     ap.add_argument("--sample-decades", type=int, default=0,
                     help="search this many random decades per configuration (0: every decade)")
-    ap.add_argument("--accept", choices=["theta", "functional"], default="theta",
+    ap.add_argument("--accept", choices=["theta", "functional"], default="functional",
                     help="acceptance test of the Fourier-accelerated steps (survey, train, compare)")
     ap.add_argument("--alphas", default=None, help="train: comma-separated step sizes of the family search")
     ap.add_argument("--highs", default=None, help="train: comma-separated high-mode factors of the family search")
