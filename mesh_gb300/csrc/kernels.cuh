@@ -795,7 +795,7 @@ template <class T, int ND, int NA> struct SiteAcc<T, ND, NA, true>
 // momenta when want_kin (the FP64 sum costs FP64-pipe time: only the last
 // momentum step of a trajectory asks for it). Shared by k_momentum_step_site
 // and the batched replicas.
-template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD, bool SM = false>
+template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD, bool SM = false, bool PIPE = false>
 __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld,
                                           T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
                                           bool want_kin, T *acc_sm = nullptr)
@@ -806,6 +806,73 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	constexpr int NA = Gp::NA;
 	double acc = 0.0;
 	SiteAcc<T, ND, NA, SM> F(acc_sm);
+	if constexpr (PIPE && ROWS && GRP == SU3 && ND == 4)
+	{
+		// software-pipelined form: the neighbour rows of the next plane (of
+		// the next lower staple) are loaded while the current one is
+		// multiplied; row 2 is rebuilt once the rows have arrived
+		E bn = ld.rows(1, eo_shift1<ND>(g, st, 0, +1)), cn = ld.rows(0, eo_shift1<ND>(g, st, 1, +1));
+#pragma unroll 1
+		for (int q = 0; q < 6; ++q)
+		{
+			int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
+			E b = bn, c = cn;
+			if (q < 5)
+			{
+				int m2 = plane_mu<ND>(q + 1), n2 = plane_nu<ND>(q + 1);
+				bn = ld.rows(n2, eo_shift1<ND>(g, st, m2, +1));
+				cn = ld.rows(m2, eo_shift1<ND>(g, st, n2, +1));
+			}
+			Gp::complete_row2(b);
+			Gp::complete_row2(c);
+			E ab = Pr::mul_r2(ld.rows(mu, s), b);
+			E dc = Pr::mul_r2(ld.rows(nu, s), c);
+			E pl = Pr::mul_nd(ab, dc);
+			T xa[NA];
+			Gp::proj(pl, xa);
+			F.plane(q, xa);
+		}
+		// lower staples: pair j = 3 mu + k, nu = k < mu ? k : k + 1
+		auto pair_nu = [](int j) {
+			int mu = j / 3, k = j - 3 * (j / 3);
+			return k < mu ? k : k + 1;
+		};
+		E en, fn, hn;
+		{
+			int64_t y = eo_shift1<ND>(g, st, 1, -1);
+			en = ld.rows(0, y);
+			fn = ld.rows(1, eo_shift2<ND>(g, st, 1, -1, 0, +1));
+			hn = ld.rows(1, y);
+		}
+		E S = Gp::zero();
+#pragma unroll 1
+		for (int j = 0; j < 12; ++j)
+		{
+			int mu = j / 3, nu = pair_nu(j);
+			E e = en, f = fn, h = hn;
+			if (j < 11)
+			{
+				int m2 = (j + 1) / 3, n2 = pair_nu(j + 1);
+				int64_t y = eo_shift1<ND>(g, st, n2, -1);
+				en = ld.rows(m2, y);
+				fn = ld.rows(n2, eo_shift2<ND>(g, st, n2, -1, m2, +1));
+				hn = ld.rows(n2, y);
+			}
+			Gp::complete_row2(f);
+			Gp::complete_row2(h);
+			Gp::add_to(S, Pr::mul_dn(Pr::mul_r2(e, f), h));
+			if (j - 3 * mu == 2)
+			{
+				E W = Pr::mul(ld(mu, s), S);
+				T xa[NA];
+				Gp::proj(W, xa);
+				F.dir(mu, xa);
+				S = Gp::zero();
+			}
+		}
+	}
+	else
+	{
 	// forward plaquette loops, one per plane
 #pragma unroll 1
 	for (int q = 0; q < ND * (ND - 1) / 2; ++q)
@@ -851,6 +918,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		T xa[NA];
 		Gp::proj(W, xa);
 		F.dir(mu, xa);
+	}
 	}
 	if constexpr (!FUSE)
 	{
@@ -900,7 +968,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 }
 
 template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false,
-          bool SM = false>
+          bool SM = false, bool PIPE = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
@@ -919,8 +987,8 @@ __global__ void __launch_bounds__(NT, MINB)
 			tile_site<ND>(ts, tile, t, x);
 			Site<ND> st = site_from_coords<ND>(g, x);
 			int64_t s = eo_of<ND>(g, st);
-			acc += site_md<GRP, T, ND, F2, ROWS, FUSE, decltype(ld), SM>(g, st, s, ld, P, coef, Uout, tu, reunit,
-			                                                            kin.result != nullptr, my);
+			acc += site_md<GRP, T, ND, F2, ROWS, FUSE, decltype(ld), SM, PIPE>(g, st, s, ld, P, coef, Uout, tu,
+			                                                                  reunit, kin.result != nullptr, my);
 		}
 	}
 	if (kin.result)
@@ -1649,6 +1717,7 @@ template <int GRP, class T, int ND> struct Ops
 		int pf = 0;        // line march: L1 prefetch of the next iteration's links
 		int sm = 0;        // thread per site: force accumulators in shared memory
 		int st = 0;        // line march: own line staged in shared memory by bulk copies (L3 = 32)
+		int pipe = 0;      // thread per site: next neighbour rows loaded ahead (software pipeline)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1659,8 +1728,9 @@ template <int GRP, class T, int ND> struct Ops
 	// staples along x1 and x3 handed over), launch shapes, products and
 	// whether row 2 of whole links is read or rebuilt; 35-36: thread per site
 	// with the force accumulators in shared memory (five blocks per SM); 37:
-	// line march with the warp's own line staged by bulk copies (TMA)
-	static constexpr int kForceVariants = 38;
+	// line march with the warp's own line staged by bulk copies (TMA); 38-39:
+	// thread per site, software-pipelined neighbour loads
+	static constexpr int kForceVariants = 40;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1702,7 +1772,9 @@ template <int GRP, class T, int ND> struct Ops
 		    {3, {0, 0, 0, 0}, 128, 4, "line/128thr/4blk/f32x2/row2/pf", 1, 1, 0, 1},
 		    {2, {1, 1, 2, 3}, 128, 5, "site/tile2x2x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1},
 		    {2, {0, 2, 2, 3}, 128, 5, "site/tile1x4x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1},
-		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/tma", 1, 0, 0, 0, 0, 1}};
+		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/tma", 1, 0, 0, 0, 0, 1},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/smacc/pipe", 1, 0, 0, 0, 1, 0, 1},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/pipe", 1, 0, 0, 0, 0, 0, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1807,6 +1879,16 @@ template <int GRP, class T, int ND> struct Ops
 	{
 		if constexpr (GRP == SU3 && ROWS && F2)
 		{
+			if (fv.pipe)
+			{
+				if (fv.sm)
+					k_momentum_step_site<GRP, T, 4, 128, 4, F2, ROWS, FUSE, true, true>
+					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				else
+					k_momentum_step_site<GRP, T, 4, 128, 4, F2, ROWS, FUSE, false, true>
+					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				return;
+			}
 			if (fv.sm)
 			{
 				k_momentum_step_site<GRP, T, 4, 128, 5, F2, ROWS, FUSE, true>
@@ -1921,7 +2003,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 37; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 39; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
