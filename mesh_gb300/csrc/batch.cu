@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kChunk)
 // links of every site; reads the proposal from Unew (flip = 0) or Ut (flip =
 // 1) and writes it to the other; with KIN also the kinetic sums
 template <int GRP, class T, bool KIN>
-__global__ void __launch_bounds__(kChunk)
+__global__ void __launch_bounds__(kChunk, GRP != SU3 && sizeof(T) == 4 ? 2 : 1)
     kb_md(BatchSpace sp, double const *__restrict__ beta, double dp, double du, int flip, int reunit, BatchRed kin)
 {
 	using Gp = Group<GRP, T>;

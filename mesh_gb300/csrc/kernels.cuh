@@ -709,6 +709,101 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 		}
 }
 
+// The per-site body for the small groups (U(1), SU(2)) in four dimensions:
+// the same momentum step (and with FUSE link update) as site_md below,
+// unrolled over planes and directions, with the site's four own links held in
+// registers and the twenty neighbour indices (x + e_mu, x - e_nu,
+// x - e_nu + e_mu) computed once per site instead of once per staple: for
+// these groups the products are a few FMAs, and the index arithmetic, not the
+// arithmetic of the staples, set the instruction count.
+template <int GRP, class T, bool FUSE, class LD>
+__device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st, int64_t s, LD const &ld,
+                                                T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
+                                                bool want_kin)
+{
+	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
+	constexpr int NA = Gp::NA;
+	int32_t f[4], b[4], d[4][4];
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+	{
+		f[mu] = int32_t(eo_shift1<4>(g, st, mu, +1));
+		b[mu] = int32_t(eo_shift1<4>(g, st, mu, -1));
+	}
+#pragma unroll
+	for (int nu = 0; nu < 4; ++nu)
+#pragma unroll
+		for (int mu = 0; mu < 4; ++mu)
+			d[nu][mu] = mu == nu ? 0 : int32_t(eo_shift2<4>(g, st, nu, -1, mu, +1));
+	E u[4];
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+		u[mu] = ld(mu, s);
+	T F[4][NA];
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			F[mu][a] = T(0);
+	// forward plaquette loops: (a b)(d c)^+ closes both forward staples
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+#pragma unroll
+		for (int nu = mu + 1; nu < 4; ++nu)
+		{
+			E pl = Gp::mul_nd(Gp::mul(u[mu], ld(nu, f[mu])), Gp::mul(u[nu], ld(mu, f[nu])));
+			T xa[NA];
+			Gp::proj(pl, xa);
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+			{
+				F[mu][a] += xa[a];
+				F[nu][a] -= xa[a];
+			}
+		}
+	// lower staples, summed per link and closed with U_mu(x)
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+	{
+		E S = Gp::zero();
+#pragma unroll
+		for (int nu = 0; nu < 4; ++nu)
+		{
+			if (nu == mu)
+				continue;
+			Gp::add_to(S, Gp::mul_dn(Gp::mul(ld(mu, b[nu]), ld(nu, d[nu][mu])), ld(nu, b[nu])));
+		}
+		T xa[NA];
+		Gp::proj(Gp::mul(u[mu], S), xa);
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			F[mu][a] += xa[a];
+	}
+	double acc = 0.0;
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+	{
+		auto Pv = comp<T, NA>(P, g.V, mu);
+		T p[NA];
+		Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			p[a] -= coef * F[mu][a];
+		Pv.template store<CACHE_STREAM>(s, p);
+		if (want_kin)
+			acc += double(Gp::kin(p));
+		if constexpr (FUSE)
+		{
+			E r = Gp::mul(Gp::exp_alg(p, tu), u[mu]);
+			if (reunit)
+				r = Gp::reunit_fast(r);
+			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
+		}
+	}
+	return acc;
+}
+
 // Force accumulators F[mu][a] of the thread-per-site body: in registers, or
 // (SM) in a block of shared memory private to the thread, element (mu, a) at
 // sm[(mu NA + a) 32] past the thread's lane (a warp's 32 threads touch 32
@@ -800,6 +895,8 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
                                           T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
                                           bool want_kin, T *acc_sm = nullptr)
 {
+	if constexpr (GRP != SU3 && ND == 4 && !SM && !PIPE)
+		return site_md_small<GRP, T, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit, want_kin);
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	using Pr = Prod<GRP, T, F2>;
