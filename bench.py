@@ -572,6 +572,7 @@ def run_batch(args):
     acc = float(np.mean([b.history(r)["accept_history"][therm + args.warmup:].mean() for r in range(b.R)]))
     plaq = b.plaquettes()
     info = b.launch_info(len(d))
+    md_launch = b.md_launch()
     chains = []
     for r in range(len(dims)):
         h = mg.Hmc(ctx, 2, mg.F32, mg.Grid(dims[r]), seed=seeds[r])
@@ -594,7 +595,8 @@ def run_batch(args):
            "speedup_vs_separate": t_sep / t_batch,
            "effective_GBps": updates * bytes_per_update / t_batch / 1e9, "peak_GBps": peak,
            "physics": {"acceptance": acc, "plaquette_mean": float(plaq.mean())},
-           "gpu_launches": info["launches_per_trajectory"] * steps, "grids": info, "clocks": clk}
+           "gpu_launches": info["launches_per_trajectory"] * steps, "grids": info,
+           "md_launch": md_launch, "clocks": clk}
     print(json.dumps(out), flush=True)
     return 0
 

@@ -330,6 +330,12 @@ int mesh_batch_plaquettes(mesh_batch h, double *out);
  * persistent grids of the link and site kernels (any output may be NULL) */
 int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_deltas, int *grid_links,
                            int *grid_sites);
+/* the MD-step form the first run timed and chose: fused = 1 (momentum step
+ * and link update in one kernel) or 0 (separate kernels), -1 before the first
+ * run; the fused kernel's launch variant, its minimum resident blocks per SM
+ * (the register cap it was compiled under) and its persistent grid (any
+ * output may be NULL). No reference counterpart: the batch is new. */
+int mesh_batch_md_launch(mesh_batch h, int *fused, int *variant, int *min_blocks, int *grid);
 
 /* ---- Landau gauge fixing (src/gauge/landau.h) ----------------------------
  * g is a single-component group field (the gauge transform); U is not

@@ -127,6 +127,7 @@ SIGNATURES = {
     "mesh_batch_history": (_I, [_P, _I, _I, _I, _DP, _DP, _DP]),
     "mesh_batch_plaquettes": (_I, [_P, _DP]),
     "mesh_batch_launch_info": (_I, [_P, _IP, _I, _IP, _IP]),
+    "mesh_batch_md_launch": (_I, [_P, _IP, _IP, _IP, _IP]),
     "mesh_landau_functional": (_I, [_P, _P, _DP]),
     "mesh_landau_line_search": (_I, [_P, _P, _P, _D, _DP]),
     "mesh_landau_theta": (_I, [_P, _P, _DP]),
@@ -685,6 +686,14 @@ class HmcBatch:
         lpt, gl, gs = C.c_int(), C.c_int(), C.c_int()
         _chk(load().mesh_batch_launch_info(self.h, C.byref(lpt), n_deltas, C.byref(gl), C.byref(gs)))
         return {"launches_per_trajectory": lpt.value, "grid_links": gl.value, "grid_sites": gs.value}
+
+    def md_launch(self):
+        """the MD-step form the first run chose: fused (1) or separate kernels
+        (0; -1 before the first run), the fused kernel's launch variant, its
+        minimum resident blocks per SM and its grid"""
+        f, v, mb, g = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _chk(load().mesh_batch_md_launch(self.h, C.byref(f), C.byref(v), C.byref(mb), C.byref(g)))
+        return {"fused": f.value, "variant": v.value, "min_blocks": mb.value, "grid": g.value}
 
     def close(self):
         if getattr(self, "h", None):

@@ -43,6 +43,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <limits>
+#include <string>
 #include <vector>
 
 namespace meshgb {
@@ -317,11 +318,23 @@ __global__ void __launch_bounds__(kChunk)
 	});
 }
 
+// launch variants of the fused MD kernel. U(1)/SU(2) in FP32: 0 the
+// unrolled per-site body (whose loads the compiler hoists) under a cap of 128
+// registers (2 resident blocks of 256 per SM), 1 the same body under 80
+// registers (3 blocks, spilling), 2 the rolled generic body under 128. One
+// variant (1 block, the unrolled body for the small groups) otherwise.
+template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 3 : 1;
+template <int GRP, class T> constexpr int md_min_blocks(int v)
+{
+	return kMdVariants<GRP, T> == 1 ? 1 : (v == 1 ? 3 : 2);
+}
+template <int GRP, class T> constexpr bool md_generic(int v) { return kMdVariants<GRP, T> > 1 && v == 2; }
+
 // P -= (beta_r / (2 Nc)) dp proj(U S) fused with U' = exp(du P) U for the four
 // links of every site; reads the proposal from Unew (flip = 0) or Ut (flip =
 // 1) and writes it to the other; with KIN also the kinetic sums
-template <int GRP, class T, bool KIN>
-__global__ void __launch_bounds__(kChunk, GRP != SU3 && sizeof(T) == 4 ? 2 : 1)
+template <int GRP, class T, bool KIN, int MB, bool GENERIC>
+__global__ void __launch_bounds__(kChunk, MB)
     kb_md(BatchSpace sp, double const *__restrict__ beta, double dp, double du, int flip, int reunit, BatchRed kin)
 {
 	using Gp = Group<GRP, T>;
@@ -329,7 +342,8 @@ __global__ void __launch_bounds__(kChunk, GRP != SU3 && sizeof(T) == 4 ? 2 : 1)
 	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(flip ? rep.Ut : rep.Unew), rep.g.V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
-		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true>(rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
+		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true, decltype(ld), false, false, GENERIC>(
+		    rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
 		                                                          static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
 		                                                          reunit, KIN);
 		return KIN ? k : 0.0;
@@ -409,8 +423,12 @@ struct BatchOps
 	void (*force)(cudaStream_t, unsigned, BatchSpace, double const *, double, BatchRed, bool kin);
 	void (*plaquette)(cudaStream_t, unsigned, BatchSpace, BatchRed, bool on_new);
 	void (*md)(cudaStream_t, unsigned, BatchSpace, double const *, double dp, double du, bool flip, bool reunit,
-	           BatchRed, bool kin);
-	int (*occupancy)(int which); // resident blocks per SM of kernel `which` (0 links-type, 1 force, 2 sites, 3 md)
+	           BatchRed, bool kin, int variant);
+	// resident blocks per SM of kernel `which` (0 links-type, 1 force, 2 sites,
+	// 3 + v the fused MD kernel in launch variant v)
+	int (*occupancy)(int which);
+	int md_variants;
+	int (*md_bound)(int v); // the minimum resident blocks per SM variant v is compiled for
 };
 
 template <int GRP, class T> struct BatchImpl
@@ -459,22 +477,53 @@ template <int GRP, class T> struct BatchImpl
 			kb_plaquette<GRP, T, false><<<g, kChunk, 0, st>>>(sp, out);
 		MESH_LAUNCH_CHECK();
 	}
-	static void md(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double dp, double du, bool flip,
-	               bool reunit, BatchRed kin, bool with_kin)
+	template <int V>
+	static void md_v(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double dp, double du, bool flip,
+	                 bool reunit, BatchRed kin, bool with_kin)
 	{
+		constexpr int MB = md_min_blocks<GRP, T>(V);
+		constexpr bool GEN = md_generic<GRP, T>(V);
 		if (with_kin)
-			kb_md<GRP, T, true><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+			kb_md<GRP, T, true, MB, GEN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
 		else
-			kb_md<GRP, T, false><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+			kb_md<GRP, T, false, MB, GEN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
 		MESH_LAUNCH_CHECK();
+	}
+	static void md(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double dp, double du, bool flip,
+	               bool reunit, BatchRed kin, bool with_kin, int v)
+	{
+		if constexpr (kMdVariants<GRP, T> > 1)
+		{
+			if (v == 1)
+				return md_v<1>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
+			if (v == 2)
+				return md_v<2>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
+		}
+		md_v<0>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
+	}
+	template <int V> static int md_occupancy()
+	{
+		int n = 0;
+		MESH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true, md_min_blocks<GRP, T>(V), md_generic<GRP, T>(V)>,
+		                                                        kChunk, 0));
+		return n;
 	}
 	static int occupancy(int which)
 	{
 		int n = 0;
 		cudaError_t e;
-		if (which == 3)
-			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true>, kChunk, 0);
-		else if (which == 1)
+		if (which >= 3)
+		{
+			if constexpr (kMdVariants<GRP, T> > 1)
+			{
+				if (which == 4)
+					return md_occupancy<1>();
+				if (which == 5)
+					return md_occupancy<2>();
+			}
+			return md_occupancy<0>();
+		}
+		if (which == 1)
 			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_force<GRP, T, true>, kChunk, 0);
 		else if (which == 2)
 			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_plaquette<GRP, T, true>, kChunk, 0);
@@ -483,7 +532,9 @@ template <int GRP, class T> struct BatchImpl
 		MESH_CUDA(e);
 		return n;
 	}
-	static constexpr BatchOps ops{random_links, unit_links, refresh, evolve, force, plaquette, md, occupancy};
+	static int md_bound(int v) { return md_min_blocks<GRP, T>(v); }
+	static constexpr BatchOps ops{random_links, unit_links, refresh, evolve, force, plaquette, md, occupancy,
+	                              kMdVariants<GRP, T>, md_bound};
 };
 
 BatchOps const &batch_ops(int group, int prec)
@@ -514,9 +565,11 @@ struct mesh_batch_s
 	double *d_part = nullptr, *d_res = nullptr; // partials [G][R]; results [4][R]
 	unsigned *d_cnt = nullptr;
 	BatchSpace links{}, sites{};
-	unsigned g_links = 0, g_force = 0, g_sites = 0, g_md = 0; // grids (links space uses g_links/g_force chunks)
-	BatchSpace md_sp{};
+	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
+	unsigned g_md[3] = {};                          // grid of each launch variant of the fused MD kernel
+	BatchSpace md_sp[3]{};
 	int use_md = -1; // fused MD steps (1) or separate kernels (0), timed at the first run; -1 not yet
+	int md_var = 0;  // the fused kernel's launch variant (timed with use_md)
 	BatchSpace force_sp{};
 	int64_t count = 0;
 	bool S_valid = false;
@@ -617,7 +670,8 @@ struct mesh_batch_s
 			else if (i + 1 < n && use_md == 1)
 			{
 				// momentum step i fused with the link update i + 1
-				o.md(st, g_md, md_sp, d_beta, deltas[i], deltas[i + 1], flip, i + 1 == n - 1, red(K_NEW), i == last_p);
+				o.md(st, g_md[md_var], md_sp[md_var], d_beta, deltas[i], deltas[i + 1], flip, i + 1 == n - 1,
+				     red(K_NEW), i == last_p, md_var);
 				flip = !flip;
 				++i;
 			}
@@ -645,6 +699,20 @@ struct mesh_batch_s
 			return;
 		cudaStream_t st = ctx->stream;
 		auto const &o = ops();
+		// MESH_BATCH_MD pins the choice instead: "sep", or a fused launch variant
+		if (char const *pin = std::getenv("MESH_BATCH_MD"); pin && pin[0])
+		{
+			if (std::string(pin) == "sep")
+			{
+				use_md = 0;
+				return;
+			}
+			int v = std::atoi(pin);
+			require(v >= 0 && v < o.md_variants, "MESH_BATCH_MD: no such fused launch variant");
+			use_md = 1;
+			md_var = v;
+			return;
+		}
 		cudaEvent_t e0, e1;
 		MESH_CUDA(cudaEventCreate(&e0));
 		MESH_CUDA(cudaEventCreate(&e1));
@@ -659,10 +727,19 @@ struct mesh_batch_s
 			MESH_CUDA(cudaEventElapsedTime(&ms, e0, e1));
 			return ms;
 		};
-		float t_md = timed([&] {
-			o.md(st, g_md, md_sp, d_beta, 0.0, 0.0, false, false, red(K_NEW), false);
-			o.md(st, g_md, md_sp, d_beta, 0.0, 0.0, true, false, red(K_NEW), false);
-		});
+		float t_md = 0.f;
+		for (int v = 0; v < o.md_variants; ++v)
+		{
+			float t = timed([&] {
+				o.md(st, g_md[v], md_sp[v], d_beta, 0.0, 0.0, false, false, red(K_NEW), false, v);
+				o.md(st, g_md[v], md_sp[v], d_beta, 0.0, 0.0, true, false, red(K_NEW), false, v);
+			});
+			if (v == 0 || t < t_md)
+			{
+				t_md = t;
+				md_var = v;
+			}
+		}
 		float t_sep = timed([&] {
 			for (int k = 0; k < 2; ++k)
 			{
@@ -791,8 +868,13 @@ int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t
 		h->force_sp =
 		    mesh_batch_s::make_space(h->d_reps, nrep, false, lch, sms * std::min(8, o.occupancy(1)), &h->g_force);
 		h->sites = mesh_batch_s::make_space(h->d_reps, nrep, true, sch, sms * std::min(8, o.occupancy(2)), &h->g_sites);
-		h->md_sp = mesh_batch_s::make_space(h->d_reps, nrep, true, sch, sms * std::min(8, o.occupancy(3)), &h->g_md);
-		unsigned G = std::max({h->g_links, h->g_force, h->g_sites, h->g_md});
+		unsigned G = std::max({h->g_links, h->g_force, h->g_sites});
+		for (int v = 0; v < o.md_variants; ++v)
+		{
+			h->md_sp[v] = mesh_batch_s::make_space(h->d_reps, nrep, true, sch, sms * std::min(8, o.occupancy(3 + v)),
+			                                       &h->g_md[v]);
+			G = std::max(G, h->g_md[v]);
+		}
 		MESH_CUDA(cudaMalloc(&h->d_part, sizeof(double) * size_t(G) * nrep));
 		MESH_CUDA(cudaMalloc(&h->d_res, sizeof(double) * 4 * size_t(nrep)));
 		MESH_CUDA(cudaMemset(h->d_res, 0, sizeof(double) * 4 * size_t(nrep)));
@@ -1019,6 +1101,22 @@ int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_del
 			*grid_links = int(h->g_force);
 		if (grid_sites)
 			*grid_sites = int(h->g_sites);
+	});
+}
+
+int mesh_batch_md_launch(mesh_batch h, int *fused, int *variant, int *min_blocks, int *grid)
+{
+	return api_call([&] {
+		require(h != nullptr, "null batch");
+		int v = h->md_var;
+		if (fused)
+			*fused = h->use_md;
+		if (variant)
+			*variant = v;
+		if (min_blocks)
+			*min_blocks = h->ops().md_bound(v);
+		if (grid)
+			*grid = int(h->g_md[v]);
 	});
 }
 

@@ -890,12 +890,14 @@ template <class T, int ND, int NA> struct SiteAcc<T, ND, NA, true>
 // momenta when want_kin (the FP64 sum costs FP64-pipe time: only the last
 // momentum step of a trajectory asks for it). Shared by k_momentum_step_site
 // and the batched replicas.
-template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD, bool SM = false, bool PIPE = false>
+template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD, bool SM = false, bool PIPE = false,
+          bool GENERIC = false>
 __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld,
                                           T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
                                           bool want_kin, T *acc_sm = nullptr)
 {
-	if constexpr (GRP != SU3 && ND == 4 && !SM && !PIPE)
+	// GENERIC: the rolled plane/staple loops below for every group
+	if constexpr (GRP != SU3 && ND == 4 && !SM && !PIPE && !GENERIC)
 		return site_md_small<GRP, T, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit, want_kin);
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
@@ -1064,8 +1066,12 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	return acc;
 }
 
+} // namespace meshgb
+#include "site_pair.cuh"
+namespace meshgb {
+
 template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false,
-          bool SM = false, bool PIPE = false>
+          bool SM = false, bool PIPE = false, int PAIR = 0>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
@@ -1084,8 +1090,12 @@ __global__ void __launch_bounds__(NT, MINB)
 			tile_site<ND>(ts, tile, t, x);
 			Site<ND> st = site_from_coords<ND>(g, x);
 			int64_t s = eo_of<ND>(g, st);
-			acc += site_md<GRP, T, ND, F2, ROWS, FUSE, decltype(ld), SM, PIPE>(g, st, s, ld, P, coef, Uout, tu,
-			                                                                  reunit, kin.result != nullptr, my);
+			if constexpr (PAIR != 0 && GRP == SU3 && ROWS && ND == 4 && sizeof(T) == 4)
+				acc += site_md_pair<FUSE, decltype(ld), SM, PAIR>(g, st, s, ld, P, coef, Uout, tu, reunit,
+				                                            kin.result != nullptr, my);
+			else
+				acc += site_md<GRP, T, ND, F2, ROWS, FUSE, decltype(ld), SM, PIPE>(g, st, s, ld, P, coef, Uout, tu,
+				                                                                  reunit, kin.result != nullptr, my);
 		}
 	}
 	if (kin.result)
@@ -1815,6 +1825,7 @@ template <int GRP, class T, int ND> struct Ops
 		int sm = 0;        // thread per site: force accumulators in shared memory
 		int st = 0;        // line march: own line staged in shared memory by bulk copies (L3 = 32)
 		int pipe = 0;      // thread per site: next neighbour rows loaded ahead (software pipeline)
+		int pair = 0;      // thread per site: sections with two products per FP32x2 operation (site_md_pair)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1826,8 +1837,10 @@ template <int GRP, class T, int ND> struct Ops
 	// whether row 2 of whole links is read or rebuilt; 35-36: thread per site
 	// with the force accumulators in shared memory (five blocks per SM); 37:
 	// line march with the warp's own line staged by bulk copies (TMA); 38-39:
-	// thread per site, software-pipelined neighbour loads
-	static constexpr int kForceVariants = 40;
+	// thread per site, software-pipelined neighbour loads; 40-45: thread per
+	// site with two products per FP32x2 operation in the sections `pair`
+	// selects (1 forward loops, 2 lower staples, 4 link update)
+	static constexpr int kForceVariants = 46;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1871,7 +1884,13 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {0, 2, 2, 3}, 128, 5, "site/tile1x4x4x8/128thr/5blk/f32x2/smacc", 1, 0, 0, 0, 1},
 		    {3, {0, 0, 0, 0}, 64, 8, "line/64thr/8blk/f32x2/tma", 1, 0, 0, 0, 0, 1},
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/smacc/pipe", 1, 0, 0, 0, 1, 0, 1},
-		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/pipe", 1, 0, 0, 0, 0, 0, 1}};
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/pipe", 1, 0, 0, 0, 0, 0, 1},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/pair-update", 1, 0, 0, 0, 0, 0, 0, 4},
+		    {2, {1, 1, 2, 3}, 128, 5, "site/tile2x2x4x8/128thr/5blk/smacc/pair-update", 1, 0, 0, 0, 1, 0, 0, 4},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/smacc/pair-loops-update", 1, 0, 0, 0, 1, 0, 0, 5},
+		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk/smacc/pair-all", 1, 0, 0, 0, 1, 0, 0, 7},
+		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk/smacc/pair-loops-update", 1, 0, 0, 0, 1, 0, 0, 5},
+		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/pair-update", 1, 0, 0, 0, 0, 0, 0, 4}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1976,6 +1995,8 @@ template <int GRP, class T, int ND> struct Ops
 	{
 		if constexpr (GRP == SU3 && ROWS && F2)
 		{
+			if (fv.pair)
+				return site_pair_cfg<ROWS, FUSE>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
 			if (fv.pipe)
 			{
 				if (fv.sm)
@@ -2005,6 +2026,29 @@ template <int GRP, class T, int ND> struct Ops
 		else
 			k_momentum_step_site<GRP, T, 4, 256, 2, F2, ROWS, FUSE>
 			    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+	}
+	// the paired thread-per-site kernel's configurations (variants 40-45)
+	template <bool ROWS, bool FUSE>
+	static void site_pair_cfg(ForceVariant const &fv, unsigned b, Geom const &g, TileSpec const &ts, T const *u,
+	                          T *p, T coef, RedSlot kin, Context &c, T *uo, T tu, int reunit)
+	{
+		if constexpr (kF2 && ROWS)
+		{
+#define MESH_PAIR_LAUNCH(MB, SMA, PARTS)                                                                             \
+	k_momentum_step_site<GRP, T, 4, 128, MB, 1, ROWS, FUSE, SMA, false, PARTS>                                     \
+	    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit)
+			if (fv.pair == 4 && !fv.sm)
+				MESH_PAIR_LAUNCH(4, false, 4);
+			else if (fv.pair == 4)
+				MESH_PAIR_LAUNCH(5, true, 4);
+			else if (fv.pair == 5 && fv.minb == 4)
+				MESH_PAIR_LAUNCH(4, true, 5);
+			else if (fv.pair == 5)
+				MESH_PAIR_LAUNCH(3, true, 5);
+			else
+				MESH_PAIR_LAUNCH(3, true, 7);
+#undef MESH_PAIR_LAUNCH
+		}
 	}
 	// the line-march kernel (SU(3), four dimensions): persistent grid of at
 	// most minb blocks per SM, every warp one contiguous range of line steps
@@ -2100,7 +2144,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 39; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 45; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)

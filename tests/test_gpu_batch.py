@@ -71,6 +71,35 @@ def test_batch_matches_single_chains_fp32(ctx, g):
         h.close()
 
 
+@pytest.mark.parametrize("g", [1, 2])
+@pytest.mark.parametrize("pin", ["sep", "0", "1", "2"])
+def test_batch_md_launch_variants_match_single_chains(ctx, monkeypatch, g, pin):
+    """every MD-step form of the FP32 small-group batch (separate kernels, and
+    the fused kernel's launch variants: unrolled per-site body under 128 and
+    80 registers, rolled body), pinned through MESH_BATCH_MD, against single
+    chains with the same seeds"""
+    monkeypatch.setenv("MESH_BATCH_MD", pin)
+    d = mg.make_deltas("2lf", 0.5, 16)
+    beta = [1.0, 1.1, 0.9, 1.2, 1.05] if g == 1 else [2.25, 2.45, 2.35, 2.55, 2.4]
+    b = mg.HmcBatch(ctx, g, mg.F32, DIMS, SEEDS)
+    b.cold_start()
+    b.run(beta, d, 3, use_graph=True)
+    ml = b.md_launch()
+    assert ml["fused"] == (0 if pin == "sep" else 1)
+    if pin != "sep":
+        assert ml["variant"] == int(pin) and ml["min_blocks"] == (3 if pin == "1" else 2) and ml["grid"] > 0
+    for r, dims in enumerate(DIMS):
+        h = mg.Hmc(ctx, g, mg.F32, mg.Grid(dims), seed=SEEDS[r])
+        h.cold_start()
+        h.run(beta[r], d, 3, use_graph=True)
+        hs, hb = h.history(), b.history(r)
+        np.testing.assert_array_equal(hb["accept_history"], hs["accept_history"])
+        np.testing.assert_allclose(hb["plaq_history"], hs["plaq_history"], rtol=1e-6)
+        assert rel(b.export(r), h.U.export()) < 1e-5
+        h.close()
+    b.close()
+
+
 def test_batch_graph_equals_eager_and_cold_start(ctx):
     d = mg.make_deltas("2lf", 0.5, 16)
     beta = [2.2, 2.6, 2.4, 2.3, 2.5]
