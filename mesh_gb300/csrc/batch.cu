@@ -322,23 +322,20 @@ __global__ void __launch_bounds__(kChunk)
 // unrolled per-site body (whose loads the compiler hoists) under a cap of 128
 // registers (2 resident blocks of 256 per SM), 1 the same body under 80
 // registers (3 blocks, spilling), 2 the rolled generic body under 128, 3 the
-// unrolled body under 64 registers (4 blocks), 4 and 5 the unrolled body in
-// its lean form (own links re-read, diagonal indices computed at use) under
-// 80 and 64 registers. One variant (1 block, the unrolled body for the small
-// groups) otherwise.
-template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 6 : 1;
+// unrolled body under 64 registers (4 blocks). One variant (1 block, the
+// unrolled body for the small groups) otherwise.
+template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 4 : 1;
 template <int GRP, class T> constexpr int md_min_blocks(int v)
 {
-	constexpr int mb[6] = {2, 3, 2, 4, 3, 4};
+	constexpr int mb[4] = {2, 3, 2, 4};
 	return kMdVariants<GRP, T> == 1 ? 1 : mb[v];
 }
 template <int GRP, class T> constexpr bool md_generic(int v) { return kMdVariants<GRP, T> > 1 && v == 2; }
-template <int GRP, class T> constexpr bool md_lean(int v) { return kMdVariants<GRP, T> > 1 && v >= 4; }
 
 // P -= (beta_r / (2 Nc)) dp proj(U S) fused with U' = exp(du P) U for the four
 // links of every site; reads the proposal from Unew (flip = 0) or Ut (flip =
 // 1) and writes it to the other; with KIN also the kinetic sums
-template <int GRP, class T, bool KIN, int MB, bool GENERIC, bool LEAN>
+template <int GRP, class T, bool KIN, int MB, bool GENERIC>
 __global__ void __launch_bounds__(kChunk, MB)
     kb_md(BatchSpace sp, double const *__restrict__ beta, double dp, double du, int flip, int reunit, BatchRed kin)
 {
@@ -347,7 +344,7 @@ __global__ void __launch_bounds__(kChunk, MB)
 	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(flip ? rep.Ut : rep.Unew), rep.g.V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
-		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true, decltype(ld), false, false, GENERIC, LEAN>(
+		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true, decltype(ld), false, false, GENERIC>(
 		    rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
 		                                                          static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
 		                                                          reunit, KIN);
@@ -488,11 +485,10 @@ template <int GRP, class T> struct BatchImpl
 	{
 		constexpr int MB = md_min_blocks<GRP, T>(V);
 		constexpr bool GEN = md_generic<GRP, T>(V);
-		constexpr bool LN = md_lean<GRP, T>(V);
 		if (with_kin)
-			kb_md<GRP, T, true, MB, GEN, LN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+			kb_md<GRP, T, true, MB, GEN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
 		else
-			kb_md<GRP, T, false, MB, GEN, LN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+			kb_md<GRP, T, false, MB, GEN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
 		MESH_LAUNCH_CHECK();
 	}
 	static void md(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double dp, double du, bool flip,
@@ -506,18 +502,13 @@ template <int GRP, class T> struct BatchImpl
 				return md_v<2>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 			if (v == 3)
 				return md_v<3>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
-			if (v == 4)
-				return md_v<4>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
-			if (v == 5)
-				return md_v<5>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 		}
 		md_v<0>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 	}
 	template <int V> static int md_occupancy()
 	{
 		int n = 0;
-		MESH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true, md_min_blocks<GRP, T>(V), md_generic<GRP, T>(V),
-		                                                              md_lean<GRP, T>(V)>,
+		MESH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true, md_min_blocks<GRP, T>(V), md_generic<GRP, T>(V)>,
 		                                                        kChunk, 0));
 		return n;
 	}
@@ -535,10 +526,6 @@ template <int GRP, class T> struct BatchImpl
 					return md_occupancy<2>();
 				if (which == 6)
 					return md_occupancy<3>();
-				if (which == 7)
-					return md_occupancy<4>();
-				if (which == 8)
-					return md_occupancy<5>();
 			}
 			return md_occupancy<0>();
 		}
@@ -585,8 +572,8 @@ struct mesh_batch_s
 	unsigned *d_cnt = nullptr;
 	BatchSpace links{}, sites{};
 	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
-	unsigned g_md[6] = {};                          // grid of each launch variant of the fused MD kernel
-	BatchSpace md_sp[6]{};
+	unsigned g_md[4] = {};                          // grid of each launch variant of the fused MD kernel
+	BatchSpace md_sp[4]{};
 	int use_md = -1; // fused MD steps (1) or separate kernels (0), timed at the first run; -1 not yet
 	int md_var = 0;  // the fused kernel's launch variant (timed with use_md)
 	BatchSpace force_sp{};

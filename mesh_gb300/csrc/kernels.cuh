@@ -716,10 +716,7 @@ template <int ND, int NA, class T> __device__ __forceinline__ void add_dir(T (&F
 // x - e_nu + e_mu) computed once per site instead of once per staple: for
 // these groups the products are a few FMAs, and the index arithmetic, not the
 // arithmetic of the staples, set the instruction count.
-// LEAN: the own links re-read (from L1) at each use and the twelve diagonal
-// neighbour indices x - e_nu + e_mu computed at their use, 28 registers
-// fewer for a register cap that would otherwise spill.
-template <int GRP, class T, bool FUSE, class LD, bool LEAN = false>
+template <int GRP, class T, bool FUSE, class LD>
 __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st, int64_t s, LD const &ld,
                                                 T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
                                                 bool want_kin)
@@ -727,40 +724,22 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	constexpr int NA = Gp::NA;
-	int32_t f[4], b[4], dd[LEAN ? 1 : 4][LEAN ? 1 : 4];
+	int32_t f[4], b[4], d[4][4];
 #pragma unroll
 	for (int mu = 0; mu < 4; ++mu)
 	{
 		f[mu] = int32_t(eo_shift1<4>(g, st, mu, +1));
 		b[mu] = int32_t(eo_shift1<4>(g, st, mu, -1));
 	}
-	if constexpr (!LEAN)
-	{
 #pragma unroll
-		for (int nu = 0; nu < 4; ++nu)
-#pragma unroll
-			for (int mu = 0; mu < 4; ++mu)
-				dd[nu][mu] = mu == nu ? 0 : int32_t(eo_shift2<4>(g, st, nu, -1, mu, +1));
-	}
-	auto d = [&](int nu, int mu) -> int32_t {
-		if constexpr (LEAN)
-			return int32_t(eo_shift2<4>(g, st, nu, -1, mu, +1));
-		else
-			return dd[nu][mu];
-	};
-	E uu[LEAN ? 1 : 4];
-	if constexpr (!LEAN)
-	{
+	for (int nu = 0; nu < 4; ++nu)
 #pragma unroll
 		for (int mu = 0; mu < 4; ++mu)
-			uu[mu] = ld(mu, s);
-	}
-	auto u = [&](int mu) -> E {
-		if constexpr (LEAN)
-			return ld(mu, s);
-		else
-			return uu[mu];
-	};
+			d[nu][mu] = mu == nu ? 0 : int32_t(eo_shift2<4>(g, st, nu, -1, mu, +1));
+	E u[4];
+#pragma unroll
+	for (int mu = 0; mu < 4; ++mu)
+		u[mu] = ld(mu, s);
 	T F[4][NA];
 #pragma unroll
 	for (int mu = 0; mu < 4; ++mu)
@@ -773,7 +752,7 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 #pragma unroll
 		for (int nu = mu + 1; nu < 4; ++nu)
 		{
-			E pl = Gp::mul_nd(Gp::mul(u(mu), ld(nu, f[mu])), Gp::mul(u(nu), ld(mu, f[nu])));
+			E pl = Gp::mul_nd(Gp::mul(u[mu], ld(nu, f[mu])), Gp::mul(u[nu], ld(mu, f[nu])));
 			T xa[NA];
 			Gp::proj(pl, xa);
 #pragma unroll
@@ -793,10 +772,10 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 		{
 			if (nu == mu)
 				continue;
-			Gp::add_to(S, Gp::mul_dn(Gp::mul(ld(mu, b[nu]), ld(nu, d(nu, mu))), ld(nu, b[nu])));
+			Gp::add_to(S, Gp::mul_dn(Gp::mul(ld(mu, b[nu]), ld(nu, d[nu][mu])), ld(nu, b[nu])));
 		}
 		T xa[NA];
-		Gp::proj(Gp::mul(u(mu), S), xa);
+		Gp::proj(Gp::mul(u[mu], S), xa);
 #pragma unroll
 		for (int a = 0; a < NA; ++a)
 			F[mu][a] += xa[a];
@@ -816,7 +795,7 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 			acc += double(Gp::kin(p));
 		if constexpr (FUSE)
 		{
-			E r = Gp::mul(Gp::exp_alg(p, tu), u(mu));
+			E r = Gp::mul(Gp::exp_alg(p, tu), u[mu]);
 			if (reunit)
 				r = Gp::reunit_fast(r);
 			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
@@ -912,14 +891,14 @@ template <class T, int ND, int NA> struct SiteAcc<T, ND, NA, true>
 // momentum step of a trajectory asks for it). Shared by k_momentum_step_site
 // and the batched replicas.
 template <int GRP, class T, int ND, int F2, bool ROWS, bool FUSE, class LD, bool SM = false, bool PIPE = false,
-          bool GENERIC = false, bool LEAN = false>
+          bool GENERIC = false>
 __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int64_t s, LD const &ld,
                                           T *__restrict__ P, T coef, T *__restrict__ Uout, T tu, int reunit,
                                           bool want_kin, T *acc_sm = nullptr)
 {
 	// GENERIC: the rolled plane/staple loops below for every group
 	if constexpr (GRP != SU3 && ND == 4 && !SM && !PIPE && !GENERIC)
-		return site_md_small<GRP, T, FUSE, LD, LEAN>(g, st, s, ld, P, coef, Uout, tu, reunit, want_kin);
+		return site_md_small<GRP, T, FUSE>(g, st, s, ld, P, coef, Uout, tu, reunit, want_kin);
 	using Gp = Group<GRP, T>;
 	using E = typename Gp::E;
 	using Pr = Prod<GRP, T, F2>;
