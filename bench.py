@@ -465,7 +465,8 @@ def run_ours(args):
                       "timing": "CUDA events on the launching stream, CUDA-graph replay of whole trajectories"},
            "physics": {"acceptance": acc, "plaquette_mean": plaq, "exp_minus_dH_mean": edH},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": ncu_traffic(f"md_step/{md_variant}"),
+                        "frac": achieved / peak,
+                        "traffic": ncu_traffic(f"md_step/{md_variant}") if list(dims) == [32] * 4 else None,
                         "kernel": KERNEL_DESC.get(md_variant.split("/")[0], md_variant) + f" [{md_variant}]",
                         "algorithmic_bytes_per_launch": B_md, "avg_launch_ms": t_md * 1e3,
                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"

@@ -321,13 +321,15 @@ __global__ void __launch_bounds__(kChunk)
 // launch variants of the fused MD kernel. U(1)/SU(2) in FP32: 0 the
 // unrolled per-site body (whose loads the compiler hoists) under a cap of 128
 // registers (2 resident blocks of 256 per SM), 1 the same body under 80
-// registers (3 blocks, spilling), 2 the rolled generic body under 128, 3 the
-// unrolled body under 64 registers (4 blocks). One variant (1 block, the
-// unrolled body for the small groups) otherwise.
-template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 4 : 1;
+// registers (3 blocks, spilling), 2 the rolled generic body under 128. One
+// variant (1 block, the unrolled body for the small groups) otherwise.
+// Measured on the 64-replica SU(2) workload: 41.9, 44.5-45.7 and 22.9 G link
+// updates/s; the unrolled body under 64 registers (4 blocks, 908 bytes of
+// spills) 30.2 G, not offered.
+template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 3 : 1;
 template <int GRP, class T> constexpr int md_min_blocks(int v)
 {
-	constexpr int mb[4] = {2, 3, 2, 4};
+	constexpr int mb[3] = {2, 3, 2};
 	return kMdVariants<GRP, T> == 1 ? 1 : mb[v];
 }
 template <int GRP, class T> constexpr bool md_generic(int v) { return kMdVariants<GRP, T> > 1 && v == 2; }
@@ -500,8 +502,6 @@ template <int GRP, class T> struct BatchImpl
 				return md_v<1>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 			if (v == 2)
 				return md_v<2>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
-			if (v == 3)
-				return md_v<3>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 		}
 		md_v<0>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 	}
@@ -524,8 +524,6 @@ template <int GRP, class T> struct BatchImpl
 					return md_occupancy<1>();
 				if (which == 5)
 					return md_occupancy<2>();
-				if (which == 6)
-					return md_occupancy<3>();
 			}
 			return md_occupancy<0>();
 		}
@@ -572,8 +570,8 @@ struct mesh_batch_s
 	unsigned *d_cnt = nullptr;
 	BatchSpace links{}, sites{};
 	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
-	unsigned g_md[4] = {};                          // grid of each launch variant of the fused MD kernel
-	BatchSpace md_sp[4]{};
+	unsigned g_md[3] = {};                          // grid of each launch variant of the fused MD kernel
+	BatchSpace md_sp[3]{};
 	int use_md = -1; // fused MD steps (1) or separate kernels (0), timed at the first run; -1 not yet
 	int md_var = 0;  // the fused kernel's launch variant (timed with use_md)
 	BatchSpace force_sp{};
