@@ -145,34 +145,13 @@ __device__ __forceinline__ double block_sum(double v)
 // for replica q the partials of the blocks that covered q's chunks [a, b):
 // all blocks when b - a >= gridDim.x, else blocks a mod G .. (b-1) mod G, in
 // that order (deterministic for a given batch).
-//
-// SREP: the block's current replica descriptor is held in shared memory
-// (copied when the replica changes, between two barriers) and the body reads
-// its geometry and pointers from there at each use, instead of keeping the
-// ~30 words live in registers for the whole loop.
-template <bool RED, bool SREP = false, class Body>
-__device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
+template <bool RED, class Body> __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
 {
 	int64_t const G = gridDim.x;
 	int64_t c = blockIdx.x;
 	int r = c < sp.nchunks ? find_rep(sp, c) : 0;
 	int64_t first = chunk0_of(sp, r), next = chunk0_of(sp, r + 1);
-	__shared__ BatchRep srep;
-	BatchRep rrep;
-	if constexpr (SREP)
-	{
-		if (threadIdx.x == 0)
-			srep = sp.reps[r];
-		__syncthreads();
-	}
-	else
-		rrep = sp.reps[r];
-	BatchRep &rep = [&]() -> BatchRep & {
-		if constexpr (SREP)
-			return srep;
-		else
-			return rrep;
-	}();
+	BatchRep rep = sp.reps[r];
 	int cur = r;
 	bool touched = false;
 	double acc = 0.0;
@@ -193,15 +172,7 @@ __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, B
 				first = next;
 				next = chunk0_of(sp, r + 1);
 			}
-			if constexpr (SREP)
-			{
-				__syncthreads(); // every thread is done with the previous replica
-				if (threadIdx.x == 0)
-					srep = sp.reps[r];
-				__syncthreads();
-			}
-			else
-				rrep = sp.reps[r];
+			rep = sp.reps[r];
 			cur = r;
 		}
 		touched = true;
@@ -350,37 +321,35 @@ __global__ void __launch_bounds__(kChunk)
 // launch variants of the fused MD kernel. U(1)/SU(2) in FP32: 0 the
 // unrolled per-site body (whose loads the compiler hoists) under a cap of 128
 // registers (2 resident blocks of 256 per SM), 1 the same body under 80
-// registers (3 blocks, spilling), 2 the rolled generic body under 128, 3 and
-// 4 the unrolled body under 80 and 64 registers with the replica descriptor
-// in shared memory (batch_loop SREP). One variant (1 block, the unrolled
-// body for the small groups) otherwise. Measured on the 64-replica SU(2)
-// workload: 41.9, 44.5-45.7 and 22.9 G link updates/s for 0-2; the unrolled
-// body under 64 registers with the descriptor in registers (908 bytes of
+// registers (3 blocks, spilling), 2 the rolled generic body under 128. One
+// variant (1 block, the unrolled body for the small groups) otherwise.
+// Measured on the 64-replica SU(2) workload: 41.9, 44.5-45.7 and 22.9 G link
+// updates/s; the unrolled body under 64 registers (4 blocks, 908 bytes of
 // spills) 30.2 G, not offered.
-template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 5 : 1;
+template <int GRP, class T> inline constexpr int kMdVariants = GRP != SU3 && sizeof(T) == 4 ? 3 : 1;
 template <int GRP, class T> constexpr int md_min_blocks(int v)
 {
-	constexpr int mb[5] = {2, 3, 2, 3, 4};
+	constexpr int mb[3] = {2, 3, 2};
 	return kMdVariants<GRP, T> == 1 ? 1 : mb[v];
 }
 template <int GRP, class T> constexpr bool md_generic(int v) { return kMdVariants<GRP, T> > 1 && v == 2; }
-template <int GRP, class T> constexpr bool md_srep(int v) { return kMdVariants<GRP, T> > 1 && v >= 3; }
 
 // P -= (beta_r / (2 Nc)) dp proj(U S) fused with U' = exp(du P) U for the four
 // links of every site; reads the proposal from Unew (flip = 0) or Ut (flip =
 // 1) and writes it to the other; with KIN also the kinetic sums
-template <int GRP, class T, bool KIN, int MB, bool GENERIC, bool SREP>
+template <int GRP, class T, bool KIN, int MB, bool GENERIC>
 __global__ void __launch_bounds__(kChunk, MB)
     kb_md(BatchSpace sp, double const *__restrict__ beta, double dp, double du, int flip, int reunit, BatchRed kin)
 {
 	using Gp = Group<GRP, T>;
 	constexpr int F2 = (GRP == SU3 && sizeof(T) == 4) ? 1 : 0;
-	batch_loop<KIN, SREP>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
+	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(flip ? rep.Ut : rep.Unew), rep.g.V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
 		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true, decltype(ld), false, false, GENERIC>(
-		    rep.g, st, s, ld, static_cast<T *>(rep.P), coef, static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
-		    reunit, KIN);
+		    rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
+		                                                          static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
+		                                                          reunit, KIN);
 		return KIN ? k : 0.0;
 	});
 }
@@ -518,11 +487,10 @@ template <int GRP, class T> struct BatchImpl
 	{
 		constexpr int MB = md_min_blocks<GRP, T>(V);
 		constexpr bool GEN = md_generic<GRP, T>(V);
-		constexpr bool SR = md_srep<GRP, T>(V);
 		if (with_kin)
-			kb_md<GRP, T, true, MB, GEN, SR><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+			kb_md<GRP, T, true, MB, GEN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
 		else
-			kb_md<GRP, T, false, MB, GEN, SR><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
+			kb_md<GRP, T, false, MB, GEN><<<g, kChunk, 0, st>>>(sp, beta, dp, du, flip ? 1 : 0, reunit ? 1 : 0, kin);
 		MESH_LAUNCH_CHECK();
 	}
 	static void md(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double dp, double du, bool flip,
@@ -534,18 +502,13 @@ template <int GRP, class T> struct BatchImpl
 				return md_v<1>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 			if (v == 2)
 				return md_v<2>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
-			if (v == 3)
-				return md_v<3>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
-			if (v == 4)
-				return md_v<4>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 		}
 		md_v<0>(st, g, sp, beta, dp, du, flip, reunit, kin, with_kin);
 	}
 	template <int V> static int md_occupancy()
 	{
 		int n = 0;
-		MESH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true, md_min_blocks<GRP, T>(V), md_generic<GRP, T>(V),
-		                                                              md_srep<GRP, T>(V)>,
+		MESH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_md<GRP, T, true, md_min_blocks<GRP, T>(V), md_generic<GRP, T>(V)>,
 		                                                        kChunk, 0));
 		return n;
 	}
@@ -561,10 +524,6 @@ template <int GRP, class T> struct BatchImpl
 					return md_occupancy<1>();
 				if (which == 5)
 					return md_occupancy<2>();
-				if (which == 6)
-					return md_occupancy<3>();
-				if (which == 7)
-					return md_occupancy<4>();
 			}
 			return md_occupancy<0>();
 		}
@@ -611,8 +570,8 @@ struct mesh_batch_s
 	unsigned *d_cnt = nullptr;
 	BatchSpace links{}, sites{};
 	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
-	unsigned g_md[5] = {};                          // grid of each launch variant of the fused MD kernel
-	BatchSpace md_sp[5]{};
+	unsigned g_md[3] = {};                          // grid of each launch variant of the fused MD kernel
+	BatchSpace md_sp[3]{};
 	int use_md = -1; // fused MD steps (1) or separate kernels (0), timed at the first run; -1 not yet
 	int md_var = 0;  // the fused kernel's launch variant (timed with use_md)
 	BatchSpace force_sp{};
