@@ -157,13 +157,22 @@ static void *mapped_host(void const *host)
 	return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+// MESH_HOST_PATH=staged: pinned host buffers too go through the staging copy
+// (one DMA copy, then the conversion kernel on the device) instead of the
+// conversion kernel reading or writing the mapped host memory
+static bool force_staged()
+{
+	char const *e = std::getenv("MESH_HOST_PATH");
+	return e && std::strcmp(e, "staged") == 0;
+}
+
 void import_host(Field &f, void const *host, size_t bytes)
 {
 	require(host != nullptr, "null host buffer");
 	require(bytes == f.host_bytes(), "host buffer size does not match the field");
 	auto &c = *f.ctx;
 	DeviceGuard dg(c.device);
-	if (void *d = mapped_host(host))
+	if (void *d = force_staged() ? nullptr : mapped_host(host))
 	{
 		ops_for(f).import_direct(f, d);
 		MESH_CUDA(cudaStreamSynchronize(c.stream));
@@ -181,7 +190,7 @@ void export_host(Field const &f, void *host, size_t bytes)
 	require(bytes == f.host_bytes(), "host buffer size does not match the field");
 	auto &c = *f.ctx;
 	DeviceGuard dg(c.device);
-	if (void *d = mapped_host(host))
+	if (void *d = force_staged() ? nullptr : mapped_host(host))
 	{
 		ops_for(f).export_direct(f, d);
 		MESH_CUDA(cudaStreamSynchronize(c.stream));

@@ -313,11 +313,12 @@ def test_run_host_roundtrip(ctx, oracle):
 
 @pytest.mark.parametrize("dims", [[4, 6, 4, 8], [4, 6, 2, 6]])
 @pytest.mark.parametrize("g,p", CASES)
-def test_pinned_host_transfers_match_staged(ctx, oracle, g, p, dims):
+def test_pinned_host_transfers_match_staged(ctx, oracle, monkeypatch, g, p, dims):
     """gauge fields and momenta through pinned host buffers (converted by the
     kernels that read and write the mapped host memory directly, 256 objects
     per block; V = 768 and V = 288, a partial last block) equal the path
-    through a staging copy, bit for bit"""
+    through a staging copy, bit for bit, and so do pinned buffers sent through
+    the staging copy (MESH_HOST_PATH=staged)"""
     torch = pytest.importorskip("torch")
     dt = mg.real_dtype(p)
     tdt = torch.float64 if p == 2 else torch.float32
@@ -336,6 +337,12 @@ def test_pinned_host_transfers_match_staged(ctx, oracle, g, p, dims):
         assert np.array_equal(out.numpy(), staged)
         if ctor is mg.GaugeField:
             assert np.array_equal(staged, host)
+        monkeypatch.setenv("MESH_HOST_PATH", "staged")
+        Fp = ctor(ctx, g, p, mg.Grid(dims)).import_(pin.numpy())
+        out2 = torch.zeros(host.shape, dtype=tdt, pin_memory=True)
+        Fp.export(out2.numpy())
+        monkeypatch.delenv("MESH_HOST_PATH")
+        assert np.array_equal(out2.numpy(), staged)
 
 
 @pytest.mark.parametrize("variant", [-1, 11, 13, 14, 15, 16, 17, 18, 20, 21, 22, 23, 25, 29, 30, 31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45])
