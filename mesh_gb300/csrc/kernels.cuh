@@ -1068,10 +1068,11 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 
 } // namespace meshgb
 #include "site_pair.cuh"
+#include "site_async.cuh"
 namespace meshgb {
 
 template <int GRP, class T, int ND, int NT, int MINB, int F2 = 0, bool ROWS = false, bool FUSE = false,
-          bool SM = false, bool PIPE = false, int PAIR = 0>
+          bool SM = false, bool PIPE = false, int PAIR = 0, bool ASYNC = false>
 __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
@@ -1080,6 +1081,9 @@ __global__ void __launch_bounds__(NT, MINB)
 	constexpr int NA = Group<GRP, T>::NA;
 	// SM: the threads' force accumulators, [warp][element][lane]
 	__shared__ T sm_acc[SM ? NT * ND * NA : 1];
+	// ASYNC: the threads' double buffers of neighbour-link rows (site_md_async)
+	constexpr bool kAsync = ASYNC && GRP == SU3 && ROWS && ND == 4 && sizeof(T) == 4;
+	__shared__ float4 abuf[kAsync ? kAsyncSmemFloat4<NT> : 1];
 	T *my = SM ? sm_acc + (threadIdx.x >> 5) * (32 * ND * NA) + (threadIdx.x & 31) : nullptr;
 	double acc = 0.0;
 	for (int tile = blockIdx.x; tile < ts.ntiles; tile += gridDim.x)
@@ -1090,7 +1094,10 @@ __global__ void __launch_bounds__(NT, MINB)
 			tile_site<ND>(ts, tile, t, x);
 			Site<ND> st = site_from_coords<ND>(g, x);
 			int64_t s = eo_of<ND>(g, st);
-			if constexpr (PAIR != 0 && GRP == SU3 && ROWS && ND == 4 && sizeof(T) == 4)
+			if constexpr (kAsync)
+				acc += site_md_async<NT, FUSE, decltype(ld), SM>(g, st, s, ld, U, P, coef, Uout, tu, reunit,
+				                                                 kin.result != nullptr, my, abuf + threadIdx.x);
+			else if constexpr (PAIR != 0 && GRP == SU3 && ROWS && ND == 4 && sizeof(T) == 4)
 				acc += site_md_pair<FUSE, decltype(ld), SM, PAIR>(g, st, s, ld, P, coef, Uout, tu, reunit,
 				                                            kin.result != nullptr, my);
 			else
@@ -1826,6 +1833,7 @@ template <int GRP, class T, int ND> struct Ops
 		int st = 0;        // line march: own line staged in shared memory by bulk copies (L3 = 32)
 		int pipe = 0;      // thread per site: next neighbour rows loaded ahead (software pipeline)
 		int pair = 0;      // thread per site: sections with two products per FP32x2 operation (site_md_pair)
+		int async = 0;     // thread per site: next step's neighbour rows copied to shared memory (site_md_async)
 	};
 	static constexpr bool kF2 = GRP == SU3 && sizeof(T) == 4;
 	// 0-10: thread per link (even/odd order or 4D tiles); 11-13: the same with
@@ -1839,8 +1847,10 @@ template <int GRP, class T, int ND> struct Ops
 	// line march with the warp's own line staged by bulk copies (TMA); 38-39:
 	// thread per site, software-pipelined neighbour loads; 40-45: thread per
 	// site with two products per FP32x2 operation in the sections `pair`
-	// selects (1 forward loops, 2 lower staples, 4 link update)
-	static constexpr int kForceVariants = 46;
+	// selects (1 forward loops, 2 lower staples, 4 link update); 46-48:
+	// thread per site with the next step's neighbour rows copied to shared
+	// memory by cp.async
+	static constexpr int kForceVariants = 49;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1890,7 +1900,10 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/smacc/pair-loops-update", 1, 0, 0, 0, 1, 0, 0, 5},
 		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk/smacc/pair-all", 1, 0, 0, 0, 1, 0, 0, 7},
 		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk/smacc/pair-loops-update", 1, 0, 0, 0, 1, 0, 0, 5},
-		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/pair-update", 1, 0, 0, 0, 0, 0, 0, 4}};
+		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/pair-update", 1, 0, 0, 0, 0, 0, 0, 4},
+		    {2, {1, 1, 2, 3}, 128, 4, "site/tile2x2x4x8/128thr/4blk/f32x2/async", 1, 0, 0, 0, 0, 0, 0, 0, 1},
+		    {2, {0, 2, 2, 3}, 128, 4, "site/tile1x4x4x8/128thr/4blk/f32x2/async", 1, 0, 0, 0, 0, 0, 0, 0, 1},
+		    {2, {1, 1, 2, 3}, 128, 3, "site/tile2x2x4x8/128thr/3blk/f32x2/async", 1, 0, 0, 0, 0, 0, 0, 0, 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -1997,6 +2010,16 @@ template <int GRP, class T, int ND> struct Ops
 		{
 			if (fv.pair)
 				return site_pair_cfg<ROWS, FUSE>(fv, b, g, ts, u, p, coef, kin, c, uo, tu, reunit);
+			if (fv.async)
+			{
+				if (fv.minb == 4)
+					k_momentum_step_site<GRP, T, 4, 128, 4, F2, ROWS, FUSE, false, false, 0, true>
+					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				else
+					k_momentum_step_site<GRP, T, 4, 128, 3, F2, ROWS, FUSE, false, false, 0, true>
+					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				return;
+			}
 			if (fv.pipe)
 			{
 				if (fv.sm)
@@ -2144,7 +2167,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 45; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 48; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
