@@ -780,7 +780,7 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 		for (int a = 0; a < NA; ++a)
 			F[mu][a] += xa[a];
 	}
-	double acc = 0.0;
+	T kacc = T(0); // the site's kinetic terms in the field precision, one FP64 add per site
 #pragma unroll
 	for (int mu = 0; mu < 4; ++mu)
 	{
@@ -792,7 +792,7 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 			p[a] -= coef * F[mu][a];
 		Pv.template store<CACHE_STREAM>(s, p);
 		if (want_kin)
-			acc += double(Gp::kin(p));
+			kacc += Gp::kin(p);
 		if constexpr (FUSE)
 		{
 			E r = Gp::mul(Gp::exp_alg(p, tu), u[mu]);
@@ -801,7 +801,7 @@ __device__ __forceinline__ double site_md_small(Geom const &g, Site<4> const &st
 			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
 		}
 	}
-	return acc;
+	return double(kacc);
 }
 
 // Force accumulators F[mu][a] of the thread-per-site body: in registers, or
@@ -903,7 +903,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	using E = typename Gp::E;
 	using Pr = Prod<GRP, T, F2>;
 	constexpr int NA = Gp::NA;
-	double acc = 0.0;
+	T kacc = T(0); // the site's kinetic terms in the field precision, one FP64 add per site
 	SiteAcc<T, ND, NA, SM> F(acc_sm);
 	if constexpr (PIPE && ROWS && GRP == SU3 && ND == 4)
 	{
@@ -1033,7 +1033,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 				p[a] -= coef * f[a];
 			Pv.template store<CACHE_STREAM>(s, p);
 			if (want_kin)
-				acc += double(Gp::kin(p));
+				kacc += Gp::kin(p);
 		}
 	}
 	else
@@ -1052,7 +1052,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 				p[a] -= coef * f[a];
 			Pv.template store<CACHE_STREAM>(s, p);
 			if (want_kin)
-				acc += double(Gp::kin(p));
+				kacc += Gp::kin(p);
 			E r;
 			if constexpr (ROWS)
 				r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
@@ -1063,7 +1063,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
 		}
 	}
-	return acc;
+	return double(kacc);
 }
 
 } // namespace meshgb

@@ -131,7 +131,7 @@ __device__ __forceinline__ double site_md_async(Geom const &g, Site<4> const &st
 			}
 		}
 	}
-	double acc = 0.0;
+	float kacc = 0.f; // the site's kinetic terms in FP32, one FP64 add per site
 #pragma unroll 1
 	for (int mu = 0; mu < 4; ++mu)
 	{
@@ -144,7 +144,7 @@ __device__ __forceinline__ double site_md_async(Geom const &g, Site<4> const &st
 			p[a] -= coef * f[a];
 		Pv.template store<CACHE_STREAM>(s, p);
 		if (want_kin)
-			acc += double(Gp::kin(p));
+			kacc += Gp::kin(p);
 		if constexpr (FUSE)
 		{
 			E r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
@@ -153,7 +153,7 @@ __device__ __forceinline__ double site_md_async(Geom const &g, Site<4> const &st
 			comp<float, Gp::NR>(Uout, V, mu).store(s, r.v);
 		}
 	}
-	return acc;
+	return double(kacc);
 }
 
 } // namespace meshgb

@@ -487,7 +487,7 @@ __device__ __forceinline__ double site_md_pair(Geom const &g, Site<4> const &st,
 			F.dir(mu, xa);
 		}
 	}
-	double acc = 0.0;
+	float kacc = 0.f; // the site's kinetic terms in FP32, one FP64 add per site
 	if constexpr (PARTS & 4)
 	{
 		// directions m and m + 2
@@ -509,7 +509,7 @@ __device__ __forceinline__ double site_md_pair(Geom const &g, Site<4> const &st,
 			Pa.template store<CACHE_STREAM>(s, pa);
 			Pb.template store<CACHE_STREAM>(s, pb);
 			if (want_kin)
-				acc += double(Gp::kin(pa)) + double(Gp::kin(pb));
+				kacc += Gp::kin(pa) + Gp::kin(pb);
 			if constexpr (FUSE)
 			{
 				M2 ex = pair::exp_alg(pa, pb, tu);
@@ -543,7 +543,7 @@ __device__ __forceinline__ double site_md_pair(Geom const &g, Site<4> const &st,
 				p[a] -= coef * f[a];
 			Pv.template store<CACHE_STREAM>(s, p);
 			if (want_kin)
-				acc += double(Gp::kin(p));
+				kacc += Gp::kin(p);
 			if constexpr (FUSE)
 			{
 				E r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
@@ -553,7 +553,7 @@ __device__ __forceinline__ double site_md_pair(Geom const &g, Site<4> const &st,
 			}
 		}
 	}
-	return acc;
+	return double(kacc);
 }
 
 } // namespace meshgb
