@@ -143,8 +143,8 @@ __device__ __forceinline__ double block_sum(double v)
 // With RED, a block's sum over one replica's chunks is flushed when the
 // replica changes (each (block, replica) pair once), and the last block adds
 // for replica q the partials of the blocks that covered q's chunks [a, b):
-// all blocks when b - a >= gridDim.x, else blocks a mod G .. (b-1) mod G, in
-// that order (deterministic for a given batch).
+// all blocks when b - a >= gridDim.x, else blocks a mod G .. (b-1) mod G
+// (one warp per replica, in a fixed order: deterministic for a given batch).
 template <bool RED, class Body> __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
 {
 	int64_t const G = gridDim.x;
@@ -221,18 +221,26 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 		__syncthreads();
 		if (is_last)
 		{
+			// one warp per replica: lane l adds the covering blocks' partials
+			// l, l + 32, ... (blocks a mod G, a+1 mod G, ... in that order),
+			// then the warp's shuffle tree: a fixed order, and the partials'
+			// load latency paid once per 32 instead of once per partial
 			__threadfence();
-			for (int q = threadIdx.x; q < sp.R; q += blockDim.x)
+			int lane = threadIdx.x & 31;
+			for (int q = threadIdx.x >> 5; q < sp.R; q += kChunk / 32)
 			{
 				int64_t a = chunk0_of(sp, q), b = chunk0_of(sp, q + 1);
+				int64_t n = b - a >= G ? G : b - a;
+				int64_t k0 = b - a >= G ? 0 : a % G;
 				double sum = 0.0;
-				if (b - a >= G)
-					for (int64_t k = 0; k < G; ++k)
-						sum += __ldcg(red.part + k * sp.R + q);
-				else
-					for (int64_t k = a; k < b; ++k)
-						sum += __ldcg(red.part + (k % G) * sp.R + q);
-				red.result[q] = sum;
+				for (int64_t i = lane; i < n; i += 32)
+				{
+					int64_t k = k0 + i;
+					sum += __ldcg(red.part + (k < G ? k : k - G) * sp.R + q);
+				}
+				sum = warp_sum(sum);
+				if (lane == 0)
+					red.result[q] = sum;
 			}
 		}
 	}
