@@ -119,17 +119,32 @@ bool tiles_ok(int32_t const *d)
 	return true;
 }
 
+// sum over the block (valid in thread 0); every thread must call it
+__device__ __forceinline__ double block_sum(double v)
+{
+	__shared__ double sw[kChunk / 32];
+	v = warp_sum(v);
+	__syncthreads(); // sw may still be read by a previous call
+	if ((threadIdx.x & 31) == 0)
+		sw[threadIdx.x >> 5] = v;
+	__syncthreads();
+	double t = 0.0;
+	if (threadIdx.x == 0)
+		for (int i = 0; i < kChunk / 32; ++i)
+			t += sw[i];
+	return t;
+}
+
 // Runs body(r, rep, mu, s) -> double for the chunks c = blockIdx.x + k
 // gridDim.x (the whole grid sweeps the batch together, as a grid-stride loop
 // over one lattice does, so neighbouring links are shared in L2) with mu the
 // direction plane (0 for sites) and s the even/odd site. The replica only
 // grows along a block's chunks; the descriptor is reloaded when it changes.
-// With RED, each warp's sum over one replica's chunks is flushed when the
-// replica changes (each (block, warp, replica) triple once, without a block
-// barrier), and the last block adds for replica q the warp partials of the
-// blocks that covered q's chunks [a, b): all blocks when b - a >= gridDim.x,
-// else blocks a mod G .. (b-1) mod G (one warp per replica, in a fixed
-// order: deterministic for a given batch).
+// With RED, a block's sum over one replica's chunks is flushed when the
+// replica changes (each (block, replica) pair once), and the last block adds
+// for replica q the partials of the blocks that covered q's chunks [a, b):
+// all blocks when b - a >= gridDim.x, else blocks a mod G .. (b-1) mod G
+// (one warp per replica, in a fixed order: deterministic for a given batch).
 template <bool RED, class Body> __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
 {
 	int64_t const G = gridDim.x;
@@ -140,21 +155,15 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 	int cur = r;
 	bool touched = false;
 	double acc = 0.0;
-	// a warp's sum over its chunks of one replica into its partial slot (no
-	// block barrier: the warps of a block do not wait for one another)
-	constexpr int NW = kChunk / 32;
-	auto flush = [&](double v, int q) {
-		v = warp_sum(v);
-		if ((threadIdx.x & 31) == 0)
-			red.part[(int64_t(blockIdx.x) * NW + (threadIdx.x >> 5)) * sp.R + q] = v;
-	};
 	for (; c < sp.nchunks; c += G)
 	{
 		if (c >= next)
 		{
 			if constexpr (RED)
 			{
-				flush(acc, cur);
+				double t = block_sum(acc);
+				if (threadIdx.x == 0)
+					red.part[int64_t(blockIdx.x) * sp.R + cur] = t;
 				acc = 0.0;
 			}
 			while (c >= next)
@@ -197,36 +206,37 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 	if constexpr (RED)
 	{
 		if (touched)
-			flush(acc, cur);
-		__threadfence();
-		__syncthreads();
+		{
+			double t = block_sum(acc);
+			if (threadIdx.x == 0)
+				red.part[int64_t(blockIdx.x) * sp.R + cur] = t;
+		}
 		__shared__ bool is_last;
 		if (threadIdx.x == 0)
 		{
+			__threadfence();
 			unsigned prev = atomicInc(red.counter, gridDim.x - 1);
 			is_last = (prev == gridDim.x - 1);
 		}
 		__syncthreads();
 		if (is_last)
 		{
-			// one warp per replica: lane l adds the warp partials l, l + 32,
-			// ... of the covering blocks (blocks a mod G, a+1 mod G, ..., each
-			// with its NW warps in order), then the warp's shuffle tree: a
-			// fixed order, and the partials' load latency paid once per 32
-			// instead of once per partial
+			// one warp per replica: lane l adds the covering blocks' partials
+			// l, l + 32, ... (blocks a mod G, a+1 mod G, ... in that order),
+			// then the warp's shuffle tree: a fixed order, and the partials'
+			// load latency paid once per 32 instead of once per partial
 			__threadfence();
 			int lane = threadIdx.x & 31;
-			for (int q = threadIdx.x >> 5; q < sp.R; q += NW)
+			for (int q = threadIdx.x >> 5; q < sp.R; q += kChunk / 32)
 			{
 				int64_t a = chunk0_of(sp, q), b = chunk0_of(sp, q + 1);
-				int64_t n = (b - a >= G ? G : b - a) * NW;
+				int64_t n = b - a >= G ? G : b - a;
 				int64_t k0 = b - a >= G ? 0 : a % G;
 				double sum = 0.0;
 				for (int64_t i = lane; i < n; i += 32)
 				{
-					int64_t k = k0 + i / NW;
-					int64_t w = i - (i / NW) * NW;
-					sum += __ldcg(red.part + ((k < G ? k : k - G) * NW + w) * sp.R + q);
+					int64_t k = k0 + i;
+					sum += __ldcg(red.part + (k < G ? k : k - G) * sp.R + q);
 				}
 				sum = warp_sum(sum);
 				if (lane == 0)
@@ -564,7 +574,7 @@ struct mesh_batch_s
 	HmcRecordDev *d_hist = nullptr;
 	int hist_cap = 0;
 	double *d_beta = nullptr;
-	double *d_part = nullptr, *d_res = nullptr; // warp partials [G][kChunk / 32][R]; results [4][R]
+	double *d_part = nullptr, *d_res = nullptr; // partials [G][R]; results [4][R]
 	unsigned *d_cnt = nullptr;
 	BatchSpace links{}, sites{};
 	unsigned g_links = 0, g_force = 0, g_sites = 0; // grids (links space uses g_links/g_force chunks)
@@ -877,7 +887,7 @@ int mesh_batch_create(mesh_ctx ctxh, int group, int precision, int nrep, int32_t
 			                                       &h->g_md[v]);
 			G = std::max(G, h->g_md[v]);
 		}
-		MESH_CUDA(cudaMalloc(&h->d_part, sizeof(double) * size_t(G) * (kChunk / 32) * nrep));
+		MESH_CUDA(cudaMalloc(&h->d_part, sizeof(double) * size_t(G) * nrep));
 		MESH_CUDA(cudaMalloc(&h->d_res, sizeof(double) * 4 * size_t(nrep)));
 		MESH_CUDA(cudaMemset(h->d_res, 0, sizeof(double) * 4 * size_t(nrep)));
 		MESH_CUDA(cudaMalloc(&h->d_cnt, sizeof(unsigned) * 4));
