@@ -145,7 +145,13 @@ __device__ __forceinline__ double block_sum(double v)
 // for replica q the partials of the blocks that covered q's chunks [a, b):
 // all blocks when b - a >= gridDim.x, else blocks a mod G .. (b-1) mod G
 // (one warp per replica, in a fixed order: deterministic for a given batch).
-template <bool RED, class Body> __device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
+//
+// ACC: the type a thread sums the body's values in between two flushes (a
+// replica's chunks of one block, a few items): the field's FP32 where the
+// values are FP32 (FP64 adds cost FP64-pipe time on this part), FP64 for
+// the block sums and the final reduction either way.
+template <bool RED, class ACC = double, class Body>
+__device__ __forceinline__ void batch_loop(BatchSpace const &sp, BatchRed red, Body &&body)
 {
 	int64_t const G = gridDim.x;
 	int64_t c = blockIdx.x;
@@ -154,17 +160,17 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 	BatchRep rep = sp.reps[r];
 	int cur = r;
 	bool touched = false;
-	double acc = 0.0;
+	ACC acc = ACC(0);
 	for (; c < sp.nchunks; c += G)
 	{
 		if (c >= next)
 		{
 			if constexpr (RED)
 			{
-				double t = block_sum(acc);
+				double t = block_sum(double(acc));
 				if (threadIdx.x == 0)
 					red.part[int64_t(blockIdx.x) * sp.R + cur] = t;
-				acc = 0.0;
+				acc = ACC(0);
 			}
 			while (c >= next)
 			{
@@ -207,7 +213,7 @@ template <bool RED, class Body> __device__ __forceinline__ void batch_loop(Batch
 	{
 		if (touched)
 		{
-			double t = block_sum(acc);
+			double t = block_sum(double(acc));
 			if (threadIdx.x == 0)
 				red.part[int64_t(blockIdx.x) * sp.R + cur] = t;
 		}
@@ -275,12 +281,12 @@ template <int GRP, class T>
 __global__ void __launch_bounds__(kChunk) kb_refresh(BatchSpace sp, HmcDev const *__restrict__ dev, BatchRed kin)
 {
 	using Gp = Group<GRP, T>;
-	batch_loop<true>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &st) {
+	batch_loop<true, T>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &st) {
 		T p[Gp::DIM], o[Gp::NA];
 		normals<T, Gp::DIM>(rep.seed, TAG_MOMENTUM, uint32_t(st.lex), uint32_t(mu), dev[r].traj, p);
 		Gp::alg_from_normals(p, o);
 		comp<T, Gp::NA>(static_cast<T *>(rep.P), rep.g.V, mu).store(s, o);
-		return double(Gp::kin(o));
+		return Gp::kin(o);
 	});
 }
 
@@ -351,14 +357,13 @@ __global__ void __launch_bounds__(kChunk, MB)
 {
 	using Gp = Group<GRP, T>;
 	constexpr int F2 = (GRP == SU3 && sizeof(T) == 4) ? 1 : 0;
-	batch_loop<KIN>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
+	batch_loop<KIN, T>(sp, kin, [&](int r, BatchRep const &rep, int, int64_t s, Site<kBND> const &st) {
 		LinkLoad<GRP, T, kBND, kRows<GRP, T>> ld{static_cast<T const *>(flip ? rep.Ut : rep.Unew), rep.g.V};
 		T coef = T(beta[r] / (2.0 * Gp::NC) * dp);
 		double k = site_md<GRP, T, kBND, F2, kRows<GRP, T>, true, decltype(ld), false, false, GENERIC>(
-		    rep.g, st, s, ld, static_cast<T *>(rep.P), coef,
-		                                                          static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
-		                                                          reunit, KIN);
-		return KIN ? k : 0.0;
+		    rep.g, st, s, ld, static_cast<T *>(rep.P), coef, static_cast<T *>(flip ? rep.Unew : rep.Ut), T(du),
+		    reunit, KIN);
+		return KIN ? T(k) : T(0); // k is the site's sum in T, exactly
 	});
 }
 
