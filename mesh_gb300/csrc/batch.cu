@@ -275,23 +275,41 @@ template <int GRP, class T> __global__ void __launch_bounds__(kChunk) kb_unit_li
 	});
 }
 
-// momentum refresh from the replica's stream at its trajectory counter, and
-// the kinetic energy
-template <int GRP, class T>
-__global__ void __launch_bounds__(kChunk) kb_refresh(BatchSpace sp, HmcDev const *__restrict__ dev, BatchRed kin)
+// momentum refresh from the replica's stream at its trajectory counter and the
+// kinetic energy, fused with the trajectory's first link update U_new =
+// exp(t P) U (optionally reunitised): the momenta are not read back
+template <int GRP, class T, bool REUNIT>
+__global__ void __launch_bounds__(kChunk)
+    kb_refresh_evolve(BatchSpace sp, HmcDev const *__restrict__ dev, BatchRed kin, T t)
 {
 	using Gp = Group<GRP, T>;
+	using E = typename Gp::E;
 	batch_loop<true, T>(sp, kin, [&](int r, BatchRep const &rep, int mu, int64_t s, Site<kBND> const &st) {
+		int64_t V = rep.g.V;
 		T p[Gp::DIM], o[Gp::NA];
 		normals<T, Gp::DIM>(rep.seed, TAG_MOMENTUM, uint32_t(st.lex), uint32_t(mu), dev[r].traj, p);
 		Gp::alg_from_normals(p, o);
-		comp<T, Gp::NA>(static_cast<T *>(rep.P), rep.g.V, mu).store(s, o);
+		comp<T, Gp::NA>(static_cast<T *>(rep.P), V, mu).store(s, o);
+		E u;
+		T const *src = static_cast<T const *>(rep.U);
+		if constexpr (kRows<GRP, T>)
+		{
+			Soa<T, Gp::NR>::template load_head<12>(src + int64_t(mu) * Gp::NR * V, V, s, u.v);
+			Gp::complete_row2(u);
+		}
+		else
+			comp<T, Gp::NR>(const_cast<T *>(src), V, mu).load(s, u.v);
+		E x = Gp::mul(Gp::exp_alg(o, t), u);
+		if constexpr (REUNIT)
+			x = Gp::reunit_fast(x);
+		comp<T, Gp::NR>(static_cast<T *>(rep.Unew), V, mu).store(s, x.v);
 		return Gp::kin(o);
 	});
 }
 
-// U_new = exp(t P) (FIRST ? U : U_new), optionally reunitised
-template <int GRP, class T, bool FIRST, bool REUNIT>
+// U_new = exp(t P) U_new, optionally reunitised (the later link updates of a
+// trajectory; the first is fused with the momentum refresh)
+template <int GRP, class T, bool REUNIT>
 __global__ void __launch_bounds__(kChunk) kb_evolve(BatchSpace sp, T t)
 {
 	using Gp = Group<GRP, T>;
@@ -301,7 +319,7 @@ __global__ void __launch_bounds__(kChunk) kb_evolve(BatchSpace sp, T t)
 		T p[Gp::NA];
 		comp<T, Gp::NA>(static_cast<T *>(rep.P), V, mu).load(s, p);
 		E u;
-		T const *src = static_cast<T const *>(FIRST ? rep.U : rep.Unew);
+		T const *src = static_cast<T const *>(rep.Unew);
 		if constexpr (kRows<GRP, T>)
 		{
 			Soa<T, Gp::NR>::template load_head<12>(src + int64_t(mu) * Gp::NR * V, V, s, u.v);
@@ -435,8 +453,9 @@ struct BatchOps
 {
 	void (*random_links)(cudaStream_t, unsigned, BatchSpace);
 	void (*unit_links)(cudaStream_t, unsigned, BatchSpace);
-	void (*refresh)(cudaStream_t, unsigned, BatchSpace, HmcDev const *, BatchRed);
-	void (*evolve)(cudaStream_t, unsigned, BatchSpace, double, bool first, bool reunit);
+	// momentum refresh + kinetic sums + the first link update U_new = exp(t P) U
+	void (*refresh)(cudaStream_t, unsigned, BatchSpace, HmcDev const *, BatchRed, double t, bool reunit);
+	void (*evolve)(cudaStream_t, unsigned, BatchSpace, double, bool reunit);
 	void (*force)(cudaStream_t, unsigned, BatchSpace, double const *, double, BatchRed, bool kin);
 	void (*plaquette)(cudaStream_t, unsigned, BatchSpace, BatchRed, bool on_new);
 	void (*md)(cudaStream_t, unsigned, BatchSpace, double const *, double dp, double du, bool flip, bool reunit,
@@ -460,21 +479,21 @@ template <int GRP, class T> struct BatchImpl
 		kb_unit_links<GRP, T><<<g, kChunk, 0, st>>>(sp);
 		MESH_LAUNCH_CHECK();
 	}
-	static void refresh(cudaStream_t st, unsigned g, BatchSpace sp, HmcDev const *dev, BatchRed kin)
+	static void refresh(cudaStream_t st, unsigned g, BatchSpace sp, HmcDev const *dev, BatchRed kin, double t,
+	                    bool reunit)
 	{
-		kb_refresh<GRP, T><<<g, kChunk, 0, st>>>(sp, dev, kin);
+		if (reunit)
+			kb_refresh_evolve<GRP, T, true><<<g, kChunk, 0, st>>>(sp, dev, kin, T(t));
+		else
+			kb_refresh_evolve<GRP, T, false><<<g, kChunk, 0, st>>>(sp, dev, kin, T(t));
 		MESH_LAUNCH_CHECK();
 	}
-	static void evolve(cudaStream_t st, unsigned g, BatchSpace sp, double t, bool first, bool reunit)
+	static void evolve(cudaStream_t st, unsigned g, BatchSpace sp, double t, bool reunit)
 	{
-		if (first && reunit)
-			kb_evolve<GRP, T, true, true><<<g, kChunk, 0, st>>>(sp, T(t));
-		else if (first)
-			kb_evolve<GRP, T, true, false><<<g, kChunk, 0, st>>>(sp, T(t));
-		else if (reunit)
-			kb_evolve<GRP, T, false, true><<<g, kChunk, 0, st>>>(sp, T(t));
+		if (reunit)
+			kb_evolve<GRP, T, true><<<g, kChunk, 0, st>>>(sp, T(t));
 		else
-			kb_evolve<GRP, T, false, false><<<g, kChunk, 0, st>>>(sp, T(t));
+			kb_evolve<GRP, T, false><<<g, kChunk, 0, st>>>(sp, T(t));
 		MESH_LAUNCH_CHECK();
 	}
 	static void force(cudaStream_t st, unsigned g, BatchSpace sp, double const *beta, double delta, BatchRed kin,
@@ -545,7 +564,7 @@ template <int GRP, class T> struct BatchImpl
 		else if (which == 2)
 			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_plaquette<GRP, T, true>, kChunk, 0);
 		else
-			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_evolve<GRP, T, false, true>, kChunk, 0);
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kb_evolve<GRP, T, true>, kChunk, 0);
 		MESH_CUDA(e);
 		return n;
 	}
@@ -666,7 +685,8 @@ struct mesh_batch_s
 			o.plaquette(st, g_sites, sites, red(S_CUR), false);
 			S_valid = true;
 		}
-		o.refresh(st, g_links, links, d_dev, red(K_OLD));
+		// the momenta and the first link update (step 0) in one pass
+		o.refresh(st, g_links, links, d_dev, red(K_OLD), deltas[0], n == 1);
 		int last_p = n >= 3 ? n - 2 : -1;
 		bool flip = false; // the proposal is in Ut
 		auto unflip = [&] {
@@ -682,7 +702,8 @@ struct mesh_batch_s
 			if (i % 2 == 0)
 			{
 				unflip();
-				o.evolve(st, g_links, links, deltas[i], i == 0, i == n - 1);
+				if (i > 0)
+					o.evolve(st, g_links, links, deltas[i], i == n - 1);
 			}
 			else if (i + 1 < n && use_md == 1)
 			{
@@ -761,7 +782,7 @@ struct mesh_batch_s
 			for (int k = 0; k < 2; ++k)
 			{
 				o.force(st, g_force, force_sp, d_beta, 0.0, red(K_NEW), false);
-				o.evolve(st, g_links, links, 0.0, false, false);
+				o.evolve(st, g_links, links, 0.0, false);
 			}
 		});
 		cudaEventDestroy(e0);
@@ -1108,12 +1129,13 @@ int mesh_batch_launch_info(mesh_batch h, int *launches_per_trajectory, int n_del
 	return api_call([&] {
 		require(h != nullptr, "null batch");
 		require(n_deltas >= 1 && n_deltas % 2 == 1, "step table length must be odd");
-		// fused: refresh + the first link update + (n - 1) / 2 fused MD steps
-		// (+ the pointer swap when that count is odd) + plaquette + Metropolis;
-		// separate: refresh + n MD steps + plaquette + Metropolis
+		// fused: refresh with the first link update + (n - 1) / 2 fused MD
+		// steps (+ the pointer swap when that count is odd) + plaquette +
+		// Metropolis; separate: refresh with the first link update + the other
+		// n - 1 MD steps + plaquette + Metropolis
 		int n_md = (n_deltas - 1) / 2;
 		if (launches_per_trajectory)
-			*launches_per_trajectory = h->use_md == 1 ? 1 + 1 + n_md + (n_md % 2) + 1 + 1 : n_deltas + 3;
+			*launches_per_trajectory = h->use_md == 1 ? 1 + n_md + (n_md % 2) + 1 + 1 : n_deltas + 2;
 		if (grid_links)
 			*grid_links = int(h->g_force);
 		if (grid_sites)
