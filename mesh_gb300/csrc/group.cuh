@@ -686,6 +686,24 @@ template <class T> struct Group<SU3, T>
 		}
 		return o;
 	}
+	// proj of a special unitary matrix given by rows 0 and 1 only: the row-2
+	// entries proj reads (a_20, a_21, Im a_22) from conj(row0 x row1)
+	MESH_HD static void proj_rows01(E const &a, T *o)
+	{
+		cx<T> a20 = cconj(csub(cmul(a.at(0, 1), a.at(1, 2)), cmul(a.at(0, 2), a.at(1, 1))));
+		cx<T> a21 = cconj(csub(cmul(a.at(0, 2), a.at(1, 0)), cmul(a.at(0, 0), a.at(1, 2))));
+		// Im a_22 = -Im(a_00 a_11 - a_01 a_10)
+		T im22 = -((a.v[0] * a.v[9] + a.v[1] * a.v[8]) - (a.v[2] * a.v[7] + a.v[3] * a.v[6]));
+		T t = (a.v[1] + a.v[9] + im22) * T(1.0 / 3.0);
+		o[0] = a.v[1] - t;
+		o[1] = a.v[9] - t;
+		o[2] = (a.v[2] - a.v[6]) * T(0.5);
+		o[3] = (a.v[3] + a.v[7]) * T(0.5);
+		o[4] = (a.v[4] - a20.re) * T(0.5);
+		o[5] = (a.v[5] + a20.im) * T(0.5);
+		o[6] = (a.v[10] - a21.re) * T(0.5);
+		o[7] = (a.v[11] + a21.im) * T(0.5);
+	}
 	// row 2 of a special unitary matrix from rows 0 and 1: conj(row0 x row1)
 	MESH_HD static void complete_row2(E &r)
 	{
@@ -848,10 +866,10 @@ struct Su3F2
 		    [&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
 		    [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
 	}
-	// a b^dagger: B(k,j) = conj(b_jk)
-	__device__ __forceinline__ static E mul_nd(E const &a, E const &b)
+	// a b^dagger: B(k,j) = conj(b_jk) (rows 0 .. NRW-1)
+	template <int NRW = 3> __device__ __forceinline__ static E mul_nd(E const &a, E const &b)
 	{
-		return prod<3>(
+		return prod<NRW>(
 		    [&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
 		    [&](int k, int j, float &re, float &im) { re = b.v[6 * j + 2 * k]; im = -b.v[6 * j + 2 * k + 1]; });
 	}

@@ -495,7 +495,10 @@ struct ProdF2
 	using E = Group<SU3, float>::E;
 	using S = Su3F2;
 	__device__ __forceinline__ static E mul(E const &a, E const &b) { return S::template mul<3>(a, b); }
-	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return S::mul_nd(a, b); }
+	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return S::template mul_nd<3>(a, b); }
+	// rows 0, 1 of a b and of a b^dagger (row 2 left unset)
+	__device__ __forceinline__ static E mul_rows(E const &a, E const &b) { return S::template mul<2>(a, b); }
+	__device__ __forceinline__ static E mul_nd_rows(E const &a, E const &b) { return S::template mul_nd<2>(a, b); }
 	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return S::mul_dn(a, b); }
 	__device__ __forceinline__ static E mul_r2(E const &a, E const &b)
 	{
@@ -978,20 +981,31 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	{
 		int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
 		E ab, dc;
-		if constexpr (ROWS)
+		T xa[NA];
+		if constexpr (ROWS && F2 && GRP == SU3)
 		{
-			// special unitary links: products from rows 0, 1 of the left factor
-			ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+			// the plaquette (a b)(d c)^+ is special unitary: rows 0, 1 of a b
+			// and of the plaquette suffice, its row-2 entries that proj reads
+			// follow from them
+			ab = ProdF2::mul_rows(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
 			dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+			Gp::proj_rows01(ProdF2::mul_nd_rows(ab, dc), xa);
 		}
 		else
 		{
-			ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-			dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+			if constexpr (ROWS)
+			{
+				// special unitary links: products from rows 0, 1 of the left factor
+				ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+				dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+			}
+			else
+			{
+				ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
+				dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+			}
+			Gp::proj(Pr::mul_nd(ab, dc), xa);
 		}
-		E pl = Pr::mul_nd(ab, dc);
-		T xa[NA];
-		Gp::proj(pl, xa);
 		F.plane(q, xa);
 	}
 	// backward staples
