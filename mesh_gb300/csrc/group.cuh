@@ -483,17 +483,18 @@ template <class T> struct Group<SU3, T>
 		return r;
 	}
 	// exp(X) for antihermitian traceless X with |X| < 1 (Frobenius norm), as
-	// the power series truncated after X^10 (remainder below |X|^11/11! =
-	// 2.5e-8) and reduced to a polynomial u0 + u1 X + u2 X^2 with the
-	// Cayley-Hamilton relation X^3 = -c1 X + i dim, c1 = |X|^2/2,
-	// i dim = det X; the series is summed by Horner's rule on the three
-	// coefficients (M. Luscher, "SU(3) matrix functions", openQCD notes). No
-	// transcendental functions: the FP32 trajectory's link update.
-	MESH_HD static E exp_series(E const &X, E const &X2, T c1, T dim)
+	// the power series truncated after X^N (N = 10: remainder below
+	// |X|^11/11! = 2.5e-8; N = 6 for |X| < 0.2: below 0.2^7/7! = 2.5e-9) and
+	// reduced to a polynomial u0 + u1 X + u2 X^2 with the Cayley-Hamilton
+	// relation X^3 = -c1 X + i dim, c1 = |X|^2/2, i dim = det X; the series
+	// is summed by Horner's rule on the three coefficients (M. Luscher,
+	// "SU(3) matrix functions", openQCD notes). No transcendental functions:
+	// the FP32 trajectory's link update.
+	template <int N = 10> MESH_HD static E exp_series(E const &X, E const &X2, T c1, T dim)
 	{
-		constexpr int N = 10;
+		static_assert(N >= 1 && N <= 10, "series order");
 		// 1/k! for k = 0..N
-		constexpr T inv_fact[N + 1] = {T(1),
+		constexpr T inv_fact[11] = {T(1),
 		                               T(1),
 		                               T(1.0 / 2),
 		                               T(1.0 / 6),
@@ -541,8 +542,13 @@ template <class T> struct Group<SU3, T>
 		T c1 = T(0.5) * kin(x);
 		T c0 = -det(X).im;
 		if constexpr (sizeof(T) == 4)
+		{
+			// |X|^2 = 2 c1: |X| < 0.2 (a molecular-dynamics step) or < 1
+			if (c1 < T(0.02))
+				return exp_series<6>(X, X2, c1, -c0);
 			if (c1 < T(0.5))
-				return exp_series(X, X2, c1, -c0);
+				return exp_series<10>(X, X2, c1, -c0);
+		}
 		cx<T> f0, f1, f2;
 		T const tiny = sizeof(T) == 8 ? T(1e-11) : T(1e-5);
 		if (c1 < tiny)
