@@ -836,6 +836,12 @@ struct Su3F2
 	// pairs of B, measured slower)
 	template <int NRW, class FA, class FB> __device__ __forceinline__ static E prod(FA fa, FB fb)
 	{
+		return prod_add<NRW, false>(E{}, fa, fb);
+	}
+	// c0 + a b (ADD) or a b, rows i < NRW: the sums start from c0's entries
+	template <int NRW, bool ADD, class FA, class FB>
+	__device__ __forceinline__ static E prod_add(E const &c0, FA fa, FB fb)
+	{
 		E r;
 #pragma unroll
 		for (int i = 0; i < NRW; ++i)
@@ -852,7 +858,7 @@ struct Su3F2
 #pragma unroll
 			for (int j = 0; j < 3; ++j)
 			{
-				unsigned long long acc = 0ull;
+				unsigned long long acc = ADD ? pk(c0.v[6 * i + 2 * j], c0.v[6 * i + 2 * j + 1]) : 0ull;
 #pragma unroll
 				for (int k = 0; k < 3; ++k)
 				{
@@ -878,6 +884,13 @@ struct Su3F2
 		return prod<NRW>(
 		    [&](int i, int k, float &re, float &im) { re = a.v[6 * i + 2 * k]; im = a.v[6 * i + 2 * k + 1]; },
 		    [&](int k, int j, float &re, float &im) { re = b.v[6 * j + 2 * k]; im = -b.v[6 * j + 2 * k + 1]; });
+	}
+	// s + a^dagger b
+	__device__ __forceinline__ static E add_dn(E const &s, E const &a, E const &b)
+	{
+		return prod_add<3, true>(
+		    s, [&](int i, int k, float &re, float &im) { re = a.v[6 * k + 2 * i]; im = -a.v[6 * k + 2 * i + 1]; },
+		    [&](int k, int j, float &re, float &im) { re = b.v[6 * k + 2 * j]; im = b.v[6 * k + 2 * j + 1]; });
 	}
 	// a^dagger b: A(i,k) = conj(a_ki)
 	__device__ __forceinline__ static E mul_dn(E const &a, E const &b)

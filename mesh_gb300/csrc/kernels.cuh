@@ -498,6 +498,8 @@ struct ProdF2
 	__device__ __forceinline__ static E mul_nd(E const &a, E const &b) { return S::template mul_nd<3>(a, b); }
 	// rows 0, 1 of a b and of a b^dagger (row 2 left unset)
 	__device__ __forceinline__ static E mul_rows(E const &a, E const &b) { return S::template mul<2>(a, b); }
+	// s + a^dagger b, the sum inside the products' FMA chains
+	__device__ __forceinline__ static E add_dn(E const &s, E const &a, E const &b) { return S::add_dn(s, a, b); }
 	__device__ __forceinline__ static E mul_nd_rows(E const &a, E const &b) { return S::template mul_nd<2>(a, b); }
 	__device__ __forceinline__ static E mul_dn(E const &a, E const &b) { return S::mul_dn(a, b); }
 	__device__ __forceinline__ static E mul_r2(E const &a, E const &b)
@@ -1025,7 +1027,10 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 				ef = Pr::mul_r2(ld.rows(mu, y), f);
 			else
 				ef = Pr::mul(ld(mu, y), f);
-			Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
+			if constexpr (F2 && GRP == SU3)
+				S = ProdF2::add_dn(S, ef, ld(nu, y));
+			else
+				Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
 		}
 		E W = Pr::mul(ld(mu, s), S);
 		T xa[NA];
