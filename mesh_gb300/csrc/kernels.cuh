@@ -910,6 +910,32 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	constexpr int NA = Gp::NA;
 	T kacc = T(0); // the site's kinetic terms in the field precision, one FP64 add per site
 	SiteAcc<T, ND, NA, SM> F(acc_sm);
+	// direction mu's force is complete: P_mu -= coef F_mu and, with FUSE, the
+	// link update from u = U_mu(x) (a full link)
+	auto finish = [&](int mu, E const &u) {
+		T f[NA];
+		F.get(mu, f);
+		auto Pv = comp<T, NA>(P, g.V, mu);
+		T p[NA];
+		Pv.template load<CACHE_STREAM>(s, p);
+#pragma unroll
+		for (int a = 0; a < NA; ++a)
+			p[a] -= coef * f[a];
+		Pv.template store<CACHE_STREAM>(s, p);
+		if (want_kin)
+			kacc += Gp::kin(p);
+		if constexpr (FUSE)
+		{
+			E r;
+			if constexpr (ROWS)
+				r = Pr::mul_r2(Gp::exp_alg(p, tu), u);
+			else
+				r = Gp::mul(Gp::exp_alg(p, tu), u);
+			if (reunit)
+				r = Gp::reunit_fast(r);
+			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
+		}
+	};
 	if constexpr (PIPE && ROWS && GRP == SU3 && ND == 4)
 	{
 		// software-pipelined form: the neighbour rows of the next plane (of
@@ -1032,55 +1058,20 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			else
 				Gp::add_to(S, Pr::mul_dn(ef, ld(nu, y)));
 		}
-		E W = Pr::mul(ld(mu, s), S);
+		E u = ld(mu, s);
 		T xa[NA];
-		Gp::proj(W, xa);
+		Gp::proj(Pr::mul(u, S), xa);
 		F.dir(mu, xa);
+		// the planes came first: direction mu is complete
+		finish(mu, u);
 	}
 	}
-	if constexpr (!FUSE)
-	{
-#pragma unroll
-		for (int mu = 0; mu < ND; ++mu)
-		{
-			auto Pv = comp<T, NA>(P, g.V, mu);
-			T p[NA], f[NA];
-			F.get(mu, f);
-			Pv.template load<CACHE_STREAM>(s, p);
-#pragma unroll
-			for (int a = 0; a < NA; ++a)
-				p[a] -= coef * f[a];
-			Pv.template store<CACHE_STREAM>(s, p);
-			if (want_kin)
-				kacc += Gp::kin(p);
-		}
-	}
-	else
+	if constexpr (PIPE && ROWS && GRP == SU3 && ND == 4)
 	{
 		// one copy of the exp body: rolled direction loop
 #pragma unroll 1
 		for (int mu = 0; mu < ND; ++mu)
-		{
-			T f[NA];
-			F.get(mu, f);
-			auto Pv = comp<T, NA>(P, g.V, mu);
-			T p[NA];
-			Pv.template load<CACHE_STREAM>(s, p);
-#pragma unroll
-			for (int a = 0; a < NA; ++a)
-				p[a] -= coef * f[a];
-			Pv.template store<CACHE_STREAM>(s, p);
-			if (want_kin)
-				kacc += Gp::kin(p);
-			E r;
-			if constexpr (ROWS)
-				r = Pr::mul_r2(Gp::exp_alg(p, tu), ld(mu, s));
-			else
-				r = Gp::mul(Gp::exp_alg(p, tu), ld(mu, s));
-			if (reunit)
-				r = Gp::reunit_fast(r);
-			comp<T, Gp::NR>(Uout, g.V, mu).store(s, r.v);
-		}
+			finish(mu, ld(mu, s));
 	}
 	return double(kacc);
 }
