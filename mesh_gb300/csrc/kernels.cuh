@@ -1003,11 +1003,29 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	}
 	else
 	{
+	// the lexicographic indices of x + e_d and x - e_d, computed once per site
+	// (each is used three times)
+	int32_t fl[ND], bl[ND];
+#pragma unroll
+	for (int d = 0; d < ND; ++d)
+	{
+		fl[d] = lex_step(g, st.px, st.lex, d, +1);
+		bl[d] = lex_step(g, st.px, st.lex, d, -1);
+	}
+	auto pick = [](int32_t const(&a)[ND], int d) {
+		int32_t r = a[0];
+#pragma unroll
+		for (int k = 1; k < ND; ++k)
+			r = d == k ? a[k] : r;
+		return r;
+	};
+	int64_t const base_nb = int64_t(st.par ^ 1) * g.Vh, base_same = int64_t(st.par) * g.Vh;
 	// forward plaquette loops, one per plane
 #pragma unroll 1
 	for (int q = 0; q < ND * (ND - 1) / 2; ++q)
 	{
 		int mu = plane_mu<ND>(q), nu = plane_nu<ND>(q);
+		int64_t xpmu = base_nb + (pick(fl, mu) >> 1), xpnu = base_nb + (pick(fl, nu) >> 1);
 		E ab, dc;
 		T xa[NA];
 		if constexpr (ROWS && F2 && GRP == SU3)
@@ -1015,8 +1033,8 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			// the plaquette (a b)(d c)^+ is special unitary: rows 0, 1 of a b
 			// and of the plaquette suffice, its row-2 entries that proj reads
 			// follow from them
-			ab = ProdF2::mul_rows(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-			dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+			ab = ProdF2::mul_rows(ld.rows(mu, s), ld(nu, xpmu));
+			dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, xpnu));
 			Gp::proj_rows01(ProdF2::mul_nd_rows(ab, dc), xa);
 		}
 		else
@@ -1024,13 +1042,13 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			if constexpr (ROWS)
 			{
 				// special unitary links: products from rows 0, 1 of the left factor
-				ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-				dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+				ab = Pr::mul_r2(ld.rows(mu, s), ld(nu, xpmu));
+				dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, xpnu));
 			}
 			else
 			{
-				ab = Pr::mul(ld(mu, s), ld(nu, eo_shift1<ND>(g, st, mu, +1)));
-				dc = Pr::mul(ld(nu, s), ld(mu, eo_shift1<ND>(g, st, nu, +1)));
+				ab = Pr::mul(ld(mu, s), ld(nu, xpmu));
+				dc = Pr::mul(ld(nu, s), ld(mu, xpnu));
 			}
 			Gp::proj(Pr::mul_nd(ab, dc), xa);
 		}
@@ -1046,8 +1064,9 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		{
 			if (nu == mu)
 				continue;
-			int64_t y = eo_shift1<ND>(g, st, nu, -1);
-			E f = ld(nu, eo_shift2<ND>(g, st, nu, -1, mu, +1));
+			int32_t lnu = pick(bl, nu);
+			int64_t y = base_nb + (lnu >> 1);
+			E f = ld(nu, base_same + (lex_step(g, st.px, lnu, mu, +1) >> 1));
 			E ef;
 			if constexpr (ROWS)
 				ef = Pr::mul_r2(ld.rows(mu, y), f);
