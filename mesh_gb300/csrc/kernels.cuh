@@ -660,8 +660,12 @@ template <int ND> __device__ __forceinline__ void tile_site(TileSpec const &ts, 
 }
 
 // planes mu < nu numbered q = 0 .. ND(ND-1)/2 - 1 in the order (0,1), (0,2), ...
+// (four dimensions: read from packed 4-bit tables, two integer operations for
+// a runtime plane)
 template <int ND> __host__ __device__ constexpr int plane_mu(int q)
 {
+	if constexpr (ND == 4)
+		return (0x211000 >> (4 * q)) & 15;
 	int mu = 0;
 	while (q >= ND - 1 - mu)
 	{
@@ -672,6 +676,8 @@ template <int ND> __host__ __device__ constexpr int plane_mu(int q)
 }
 template <int ND> __host__ __device__ constexpr int plane_nu(int q)
 {
+	if constexpr (ND == 4)
+		return (0x332321 >> (4 * q)) & 15;
 	int mu = 0;
 	while (q >= ND - 1 - mu)
 	{
