@@ -430,6 +430,38 @@ template <int GRP, class T, int ND, bool ROWS = false> struct LinkLoad
 	}
 };
 
+// SU(3) FP32 rows-0,1 loads with 32-bit offsets in float4 units (the
+// thread-per-site kernel: one wide multiply-add per float4 instead of 64-bit
+// index arithmetic); valid while 18 V < 2^32 float4s (V < 238 M sites)
+struct LinkLoadSU3R32
+{
+	using E = Group<SU3, float>::E;
+	float4 const *U4;
+	uint32_t V, Vmu; // sites per parity plane pair; float4s per direction (4.5 V)
+	__host__ __device__ static bool fits(int64_t V) { return 18 * V < (int64_t(1) << 32); }
+	__device__ __forceinline__ E rows(int mu, int64_t s) const
+	{
+		uint32_t o = uint32_t(mu) * Vmu + uint32_t(s);
+		E e;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			float4 t = ld4<CACHE_KEEP>(U4 + (o + uint32_t(k) * V));
+			e.v[4 * k] = t.x;
+			e.v[4 * k + 1] = t.y;
+			e.v[4 * k + 2] = t.z;
+			e.v[4 * k + 3] = t.w;
+		}
+		return e;
+	}
+	__device__ __forceinline__ E operator()(int mu, int64_t s) const
+	{
+		E e = rows(mu, s);
+		Group<SU3, float>::complete_row2(e);
+		return e;
+	}
+};
+
 // rebuilt-row link loads for SU(3) in FP32 (the mixed-precision HMC links)
 template <int GRP, class T> inline constexpr bool kRows = GRP == SU3 && sizeof(T) == 4;
 
@@ -1112,7 +1144,14 @@ __global__ void __launch_bounds__(NT, MINB)
     k_momentum_step_site(Geom g, TileSpec ts, T const *__restrict__ U, T *__restrict__ P, T coef, RedSlot kin,
                          T *__restrict__ Uout = nullptr, T tu = T(0), int reunit = 0)
 {
-	LinkLoad<GRP, T, ND, ROWS> ld{U, g.V};
+	constexpr bool kR32 = GRP == SU3 && ROWS && ND == 4 && sizeof(T) == 4;
+	using LD = std::conditional_t<kR32, LinkLoadSU3R32, LinkLoad<GRP, T, ND, ROWS>>;
+	LD ld = [&] {
+		if constexpr (kR32)
+			return LinkLoadSU3R32{reinterpret_cast<float4 const *>(U), uint32_t(g.V), uint32_t(g.V / 2 * 9)};
+		else
+			return LinkLoad<GRP, T, ND, ROWS>{U, g.V};
+	}();
 	constexpr int NA = Group<GRP, T>::NA;
 	// SM: the threads' force accumulators, [warp][element][lane]
 	__shared__ T sm_acc[SM ? NT * ND * NA : 1];
@@ -1960,6 +1999,8 @@ template <int GRP, class T, int ND> struct Ops
 			return GRP == SU3 && ND == 4 && line_supported(g) && (!fv.st || (kF2 && g.L[3] == 32));
 		if (ND != 4)
 			return false;
+		if (fv.tiled == 2 && kF2 && !LinkLoadSU3R32::fits(g.V))
+			return false; // the per-site kernel's 32-bit link offsets
 		for (int i = 0; i < 4; ++i)
 			if (g.L[i] % (1 << fv.lt[i]) != 0)
 				return false;
