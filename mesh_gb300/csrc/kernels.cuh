@@ -948,11 +948,18 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 	constexpr int NA = Gp::NA;
 	T kacc = T(0); // the site's kinetic terms in the field precision, one FP64 add per site
 	SiteAcc<T, ND, NA, SM> F(acc_sm);
-	// direction mu's force is complete: P_mu -= coef F_mu and, with FUSE, the
-	// link update from u = U_mu(x) (a full link)
-	auto finish = [&](int mu, E const &u) {
+	// direction mu's force is complete (F_mu plus `last`, its lower-staple
+	// term, when given): P_mu -= coef F_mu and, with FUSE, the link update
+	// from u = U_mu(x) (a full link)
+	auto finish = [&](int mu, E const &u, T const *last) {
 		T f[NA];
 		F.get(mu, f);
+		if (last)
+		{
+#pragma unroll
+			for (int a = 0; a < NA; ++a)
+				f[a] += last[a];
+		}
 		auto Pv = comp<T, NA>(P, g.V, mu);
 		T p[NA];
 		Pv.template load<CACHE_STREAM>(s, p);
@@ -1118,9 +1125,8 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		E u = ld(mu, s);
 		T xa[NA];
 		Gp::proj(Pr::mul(u, S), xa);
-		F.dir(mu, xa);
 		// the planes came first: direction mu is complete
-		finish(mu, u);
+		finish(mu, u, xa);
 	}
 	}
 	if constexpr (PIPE && ROWS && GRP == SU3 && ND == 4)
@@ -1128,7 +1134,7 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		// one copy of the exp body: rolled direction loop
 #pragma unroll 1
 		for (int mu = 0; mu < ND; ++mu)
-			finish(mu, ld(mu, s));
+			finish(mu, ld(mu, s), nullptr);
 	}
 	return double(kacc);
 }
