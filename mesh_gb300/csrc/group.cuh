@@ -713,9 +713,27 @@ template <class T> struct Group<SU3, T>
 	// row 2 of a special unitary matrix from rows 0 and 1: conj(row0 x row1)
 	MESH_HD static void complete_row2(E &r)
 	{
-		r.set(2, 0, cconj(csub(cmul(r.at(0, 1), r.at(1, 2)), cmul(r.at(0, 2), r.at(1, 1)))));
-		r.set(2, 1, cconj(csub(cmul(r.at(0, 2), r.at(1, 0)), cmul(r.at(0, 0), r.at(1, 2)))));
-		r.set(2, 2, cconj(csub(cmul(r.at(0, 0), r.at(1, 1)), cmul(r.at(0, 1), r.at(1, 0)))));
+		if constexpr (sizeof(T) == 4)
+		{
+			// entry j = conj(a_0k a_1l - a_0l a_1k), (k, l) = (1, 2), (2, 0),
+			// (0, 1): each real part one multiply and three fused multiply-adds
+			auto entry = [&](int j, int k, int l) {
+				T xr = r.v[2 * k], xi = r.v[2 * k + 1], yr = r.v[6 + 2 * l], yi = r.v[6 + 2 * l + 1];
+				T ur = r.v[2 * l], ui = r.v[2 * l + 1], vr = r.v[6 + 2 * k], vi = r.v[6 + 2 * k + 1];
+				// re(z) = xr yr - xi yi - ur vr + ui vi;  -im(z) = -xr yi - xi yr + ur vi + ui vr
+				r.v[12 + 2 * j] = fmaf(xr, yr, fmaf(-xi, yi, fmaf(-ur, vr, ui * vi)));
+				r.v[12 + 2 * j + 1] = fmaf(-xr, yi, fmaf(-xi, yr, fmaf(ur, vi, ui * vr)));
+			};
+			entry(0, 1, 2);
+			entry(1, 2, 0);
+			entry(2, 0, 1);
+		}
+		else
+		{
+			r.set(2, 0, cconj(csub(cmul(r.at(0, 1), r.at(1, 2)), cmul(r.at(0, 2), r.at(1, 1)))));
+			r.set(2, 1, cconj(csub(cmul(r.at(0, 2), r.at(1, 0)), cmul(r.at(0, 0), r.at(1, 2)))));
+			r.set(2, 2, cconj(csub(cmul(r.at(0, 0), r.at(1, 1)), cmul(r.at(0, 1), r.at(1, 0)))));
+		}
 	}
 	// exact: Gram-Schmidt rows 0,1; row 2 = conj(row0 x row1)
 	MESH_HD static E reunit_exact(E const &a)
