@@ -529,6 +529,79 @@ template <class T> struct Group<SU3, T>
 			}
 		return r;
 	}
+	// rows 0 and 1 of exp(t X) for X = from_alg(o), FP32, when |tX| < 0.2
+	// (a molecular-dynamics step; row 2 of the result left unset): the order-6
+	// series of exp_series with only the entries rows 0 and 1 read, each real
+	// part one multiply and three fused multiply-adds; exp_alg otherwise
+	MESH_HD static E exp_alg_rows01(T const *o, T t)
+	{
+		static_assert(sizeof(T) == 4, "FP32 only");
+		T x[8];
+#pragma unroll
+		for (int k = 0; k < 8; ++k)
+			x[k] = o[k] * t;
+		T c1 = T(0.5) * kin(x);
+		if (!(c1 < T(0.02)))
+			return exp_alg(o, t);
+		E X = from_alg(x);
+		// X^2 rows 0, 1 (hermitian): diagonal -sum_k |X_ik|^2, (0,1), (0,2),
+		// (1,2) multiplied out, (1,0) = conj (0,1)
+		T d0 = 0, d1 = 0;
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+		{
+			d0 = fmaf(X.v[2 * k], X.v[2 * k], fmaf(X.v[2 * k + 1], X.v[2 * k + 1], d0));
+			d1 = fmaf(X.v[6 + 2 * k], X.v[6 + 2 * k], fmaf(X.v[6 + 2 * k + 1], X.v[6 + 2 * k + 1], d1));
+		}
+		auto up = [&](int i, int j, T &re, T &im) {
+			re = 0, im = 0;
+#pragma unroll
+			for (int k = 0; k < 3; ++k)
+			{
+				T ar = X.v[6 * i + 2 * k], ai = X.v[6 * i + 2 * k + 1];
+				T br = X.v[6 * k + 2 * j], bi = X.v[6 * k + 2 * j + 1];
+				re = fmaf(ar, br, fmaf(-ai, bi, re));
+				im = fmaf(ar, bi, fmaf(ai, br, im));
+			}
+		};
+		E X2;
+		X2.v[0] = -d0, X2.v[1] = 0;
+		X2.v[8] = -d1, X2.v[9] = 0;
+		up(0, 1, X2.v[2], X2.v[3]);
+		up(0, 2, X2.v[4], X2.v[5]);
+		up(1, 2, X2.v[10], X2.v[11]);
+		X2.v[6] = X2.v[2], X2.v[7] = -X2.v[3];
+		// i dim = det X
+		T dim = det(X).im;
+		constexpr int N = 6;
+		constexpr T inv_fact[N + 1] = {T(1), T(1), T(1.0 / 2), T(1.0 / 6), T(1.0 / 24), T(1.0 / 120), T(1.0 / 720)};
+		T u0r = inv_fact[N], u0i = 0, u1r = 0, u1i = 0, u2r = 0, u2i = 0;
+#pragma unroll
+		for (int k = N - 1; k >= 0; --k)
+		{
+			T n0r = fmaf(-dim, u2i, inv_fact[k]), n0i = dim * u2r;
+			T n1r = fmaf(-c1, u2r, u0r), n1i = fmaf(-c1, u2i, u0i);
+			u2r = u1r, u2i = u1i;
+			u1r = n1r, u1i = n1i;
+			u0r = n0r, u0i = n0i;
+		}
+		E r;
+#pragma unroll
+		for (int k = 0; k < 6; ++k)
+		{
+			T xr = X.v[2 * k], xi = X.v[2 * k + 1], yr = X2.v[2 * k], yi = X2.v[2 * k + 1];
+			T re = fmaf(u1r, xr, fmaf(-u1i, xi, fmaf(u2r, yr, -u2i * yi)));
+			T im = fmaf(u1r, xi, fmaf(u1i, xr, fmaf(u2r, yi, u2i * yr)));
+			if (k == 0 || k == 4)
+			{
+				re += u0r;
+				im += u0i;
+			}
+			r.v[2 * k] = re;
+			r.v[2 * k + 1] = im;
+		}
+		return r;
+	}
 	// exp(t X) for X = from_alg(o) (antihermitian traceless), Cayley-Hamilton
 	MESH_HD static E exp_alg(T const *o, T t)
 	{

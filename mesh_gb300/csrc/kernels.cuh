@@ -972,7 +972,9 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 		if constexpr (FUSE)
 		{
 			E r;
-			if constexpr (ROWS)
+			if constexpr (ROWS && GRP == SU3 && sizeof(T) == 4)
+				r = Pr::mul_r2(Gp::exp_alg_rows01(p, tu), u); // mul_r2 reads rows 0, 1 of its left factor
+			else if constexpr (ROWS)
 				r = Pr::mul_r2(Gp::exp_alg(p, tu), u);
 			else
 				r = Gp::mul(Gp::exp_alg(p, tu), u);
