@@ -1932,9 +1932,8 @@ template <int GRP, class T, int ND> struct Ops
 	// selects (1 forward loops, 2 lower staples, 4 link update); 46-48:
 	// thread per site with the next step's neighbour rows copied to shared
 	// memory by cp.async; 49-53: thread per site, more tile shapes of 512 and
-	// 256 sites; 54-56: thread per site, accumulators in shared memory, 24
-	// warps per SM
-	static constexpr int kForceVariants = 57;
+	// 256 sites
+	static constexpr int kForceVariants = 54;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1992,10 +1991,7 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 3, 4}, 512, 1, "site/tile2x2x8x16/512thr/1blk/f32x2", 1},
 		    {2, {0, 2, 3, 4}, 512, 1, "site/tile1x4x8x16/512thr/1blk/f32x2", 1},
 		    {2, {1, 2, 2, 4}, 512, 1, "site/tile2x4x4x16/512thr/1blk/f32x2", 1},
-		    {2, {1, 1, 3, 3}, 256, 2, "site/tile2x2x8x8/256thr/2blk/f32x2", 1},
-		    {2, {1, 1, 2, 3}, 128, 6, "site/tile2x2x4x8/128thr/6blk/f32x2/smacc", 1, 0, 0, 0, 1},
-		    {2, {0, 2, 2, 3}, 128, 6, "site/tile1x4x4x8/128thr/6blk/f32x2/smacc", 1, 0, 0, 0, 1},
-		    {2, {1, 2, 2, 3}, 256, 3, "site/tile2x4x4x8/256thr/3blk/f32x2/smacc", 1, 0, 0, 0, 1}};
+		    {2, {1, 1, 3, 3}, 256, 2, "site/tile2x2x8x8/256thr/2blk/f32x2", 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -2126,15 +2122,8 @@ template <int GRP, class T, int ND> struct Ops
 			}
 			if (fv.sm)
 			{
-				if (fv.threads == 256)
-					k_momentum_step_site<GRP, T, 4, 256, 3, F2, ROWS, FUSE, true>
-					    <<<b, 256, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-				else if (fv.minb == 6)
-					k_momentum_step_site<GRP, T, 4, 128, 6, F2, ROWS, FUSE, true>
-					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
-				else
-					k_momentum_step_site<GRP, T, 4, 128, 5, F2, ROWS, FUSE, true>
-					    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
+				k_momentum_step_site<GRP, T, 4, 128, 5, F2, ROWS, FUSE, true>
+				    <<<b, 128, 0, c.stream>>>(g, ts, u, p, coef, kin, uo, tu, reunit);
 				return;
 			}
 		}
@@ -2268,7 +2257,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 56; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 53; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)
