@@ -89,6 +89,13 @@ int mesh_ctx_destroy(mesh_ctx ctx);
 int mesh_ctx_synchronize(mesh_ctx ctx);
 /* the cudaStream_t the context launches on */
 void *mesh_ctx_stream(mesh_ctx ctx);
+/* Test of the bounded device-side waits (no reference counterpart): one
+ * thread waits up to `seconds` (<= 2) for a device flag that is set before
+ * the launch when flag_set != 0 and never otherwise; an expired wait is
+ * recorded in the context's device error word and returned as
+ * MESH_ERR_TIMEOUT, as the kernels with bounded waits report theirs. The
+ * context stays usable. Synchronises the context's stream. */
+int mesh_ctx_wait_probe(mesh_ctx ctx, double seconds, int flag_set);
 
 /* ---- fields: Lattice<T> / LatticeStack<T> / GaugeField<G> ---------------
  * Replaces Lattice<T>(Grid) and LatticeStack<T>(Grid)

@@ -64,6 +64,7 @@ SIGNATURES = {
     "mesh_ctx_destroy": (_I, [_P]),
     "mesh_ctx_synchronize": (_I, [_P]),
     "mesh_ctx_stream": (_P, [_P]),
+    "mesh_ctx_wait_probe": (_I, [_P, C.c_double, _I]),
     "mesh_field_create": (_I, [_P, _I, _I, _I, _I, _I32P, _I, _PP]),
     "mesh_field_destroy": (_I, [_P]),
     "mesh_field_info": (_I, [_P, _IP, _IP, _IP, _IP, _I32P, _IP]),
@@ -241,6 +242,12 @@ class Context:
 
     def synchronize(self):
         _chk(load().mesh_ctx_synchronize(self.h))
+
+    def wait_probe(self, seconds: float, flag_set: bool) -> None:
+        """a device-side wait bounded at `seconds` on a flag set before the
+        launch (flag_set) or never: raises MeshError(MESH_ERR_TIMEOUT) when
+        the wait expired"""
+        _chk(load().mesh_ctx_wait_probe(self.h, float(seconds), 1 if flag_set else 0))
 
     def close(self):
         if getattr(self, "h", None):

@@ -23,8 +23,8 @@ void meshgb::check_device_error(Context &c)
 	if (e)
 	{
 		MESH_CUDA(cudaMemsetAsync(c.d_err, 0, sizeof(int), c.stream));
-		throw Error(MESH_ERR_TIMEOUT, "a bounded device-side wait expired (TMA copy of a lattice line did not "
-		                              "complete); the launch's results are invalid");
+		throw Error(MESH_ERR_TIMEOUT, "a bounded device-side wait expired (a copy or flag it waited for did not "
+		                              "arrive); the launch's results are invalid");
 	}
 }
 
@@ -468,6 +468,53 @@ int mesh_ctx_synchronize(mesh_ctx h)
 }
 
 void *mesh_ctx_stream(mesh_ctx h) { return h ? static_cast<void *>(h->c.stream) : nullptr; }
+
+namespace {
+// one thread waits for *flag != 0, giving up after limit_ns (global timer)
+// and recording that in the context's device error word, as the kernels
+// with bounded waits do
+__global__ void k_wait_probe(unsigned const *flag, int *err, unsigned long long limit_ns)
+{
+	auto now = [] {
+		unsigned long long t;
+		asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+		return t;
+	};
+	unsigned long long t0 = now();
+	while (atomicAdd(const_cast<unsigned *>(flag), 0u) == 0u)
+	{
+		if (now() - t0 > limit_ns)
+		{
+			atomicExch(err, 1);
+			return;
+		}
+		__nanosleep(1000);
+	}
+}
+} // namespace
+
+int mesh_ctx_wait_probe(mesh_ctx h, double seconds, int flag_set)
+{
+	return api([&] {
+		require(h != nullptr, "null context");
+		require(seconds > 0 && seconds <= 2.0, "wait limit must be in (0, 2] seconds");
+		auto &c = h->c;
+		DeviceGuard dg(c.device);
+		unsigned *flag = nullptr;
+		MESH_CUDA(cudaMalloc(&flag, sizeof(unsigned)));
+		cudaError_t e = cudaMemsetAsync(flag, flag_set ? 1 : 0, sizeof(unsigned), c.stream);
+		if (e == cudaSuccess)
+		{
+			k_wait_probe<<<1, 1, 0, c.stream>>>(flag, c.d_err, (unsigned long long)(seconds * 1e9));
+			e = cudaGetLastError();
+		}
+		if (e == cudaSuccess)
+			e = cudaStreamSynchronize(c.stream);
+		cudaFree(flag);
+		MESH_CUDA(e);
+		check_device_error(c);
+	});
+}
 
 // ---- fields ----------------------------------------------------------------
 int mesh_field_create(mesh_ctx ctx, int kind, int group, int precision, int nd, int32_t const *dims, int nstack,

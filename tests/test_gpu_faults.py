@@ -74,3 +74,19 @@ def test_bad_links_reject_the_trajectory(ctx, p, fault):
     rec = h.update(BETA, d)
     assert np.isfinite(rec["dH"]) and rec["plaquette"] <= 1.0
     h.close()
+
+
+def test_bounded_wait_expires_and_the_context_stays_usable(ctx):
+    """a device-side wait on a flag that nothing sets gives up after its
+    limit and reports MESH_ERR_TIMEOUT through the context's error word; the
+    next launches on the same context run normally"""
+    import time
+    t0 = time.perf_counter()
+    with pytest.raises(mg.MeshError) as e:
+        ctx.wait_probe(0.05, flag_set=False)
+    assert e.value.code == 4  # MESH_ERR_TIMEOUT
+    assert time.perf_counter() - t0 < 5.0
+    ctx.wait_probe(0.05, flag_set=True)  # the flag is set: no wait, no error
+    ctx.synchronize()
+    U = mg.GaugeField(ctx, 3, mg.F32, mg.Grid([4, 4, 4, 4])).set_unit()
+    assert mg.plaquette(U) == pytest.approx(1.0)
