@@ -430,10 +430,6 @@ template <int GRP, class T, int ND, bool ROWS = false> struct LinkLoad
 	}
 };
 
-// the thread-per-site body reads row 2 of the plaquette loops' neighbour
-// links from memory instead of rebuilding it
-inline constexpr bool kPlaneRow2Read = true;
-
 // SU(3) FP32 rows-0,1 loads with 32-bit offsets in float4 units (the
 // thread-per-site kernel: one wide multiply-add per float4 instead of 64-bit
 // index arithmetic); valid while 18 V < 2^32 float4s (V < 238 M sites)
@@ -462,27 +458,6 @@ struct LinkLoadSU3R32
 	{
 		E e = rows(mu, s);
 		Group<SU3, float>::complete_row2(e);
-		return e;
-	}
-	// all 18 reals as stored (row 2 read, not rebuilt): the four float4 planes
-	// and the float2 tail plane of direction mu
-	__device__ __forceinline__ E full(int mu, int64_t s) const
-	{
-		uint32_t o = uint32_t(mu) * Vmu + uint32_t(s);
-		E e;
-#pragma unroll
-		for (int k = 0; k < 4; ++k)
-		{
-			float4 t = ld4<CACHE_KEEP>(U4 + (o + uint32_t(k) * V));
-			e.v[4 * k] = t.x;
-			e.v[4 * k + 1] = t.y;
-			e.v[4 * k + 2] = t.z;
-			e.v[4 * k + 3] = t.w;
-		}
-		float2 const *tail = reinterpret_cast<float2 const *>(U4 + uint32_t(mu) * Vmu + 4 * V);
-		float2 t = ld2<CACHE_KEEP>(tail + uint32_t(s));
-		e.v[16] = t.x;
-		e.v[17] = t.y;
 		return e;
 	}
 };
@@ -1105,16 +1080,8 @@ __device__ __forceinline__ double site_md(Geom const &g, Site<ND> const &st, int
 			// the plaquette (a b)(d c)^+ is special unitary: rows 0, 1 of a b
 			// and of the plaquette suffice, its row-2 entries that proj reads
 			// follow from them
-			if constexpr (std::is_same_v<LD, LinkLoadSU3R32> && kPlaneRow2Read)
-			{
-				ab = ProdF2::mul_rows(ld.rows(mu, s), ld.full(nu, xpmu));
-				dc = Pr::mul_r2(ld.rows(nu, s), ld.full(mu, xpnu));
-			}
-			else
-			{
-				ab = ProdF2::mul_rows(ld.rows(mu, s), ld(nu, xpmu));
-				dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, xpnu));
-			}
+			ab = ProdF2::mul_rows(ld.rows(mu, s), ld(nu, xpmu));
+			dc = Pr::mul_r2(ld.rows(nu, s), ld(mu, xpnu));
 			Gp::proj_rows01(ProdF2::mul_nd_rows(ab, dc), xa);
 		}
 		else
