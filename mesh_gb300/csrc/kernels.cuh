@@ -1931,9 +1931,9 @@ template <int GRP, class T, int ND> struct Ops
 	// site with two products per FP32x2 operation in the sections `pair`
 	// selects (1 forward loops, 2 lower staples, 4 link update); 46-48:
 	// thread per site with the next step's neighbour rows copied to shared
-	// memory by cp.async; 49-53: thread per site, more tile shapes of 512 and
-	// 256 sites
-	static constexpr int kForceVariants = 54;
+	// memory by cp.async; 49-53, 54-57: thread per site, more tile shapes of
+	// 512 and 256 sites
+	static constexpr int kForceVariants = 58;
 	static int n_force_variants() { return ND == 4 ? kForceVariants : 2; }
 	static ForceVariant force_variant(int v)
 	{
@@ -1991,7 +1991,11 @@ template <int GRP, class T, int ND> struct Ops
 		    {2, {1, 1, 3, 4}, 512, 1, "site/tile2x2x8x16/512thr/1blk/f32x2", 1},
 		    {2, {0, 2, 3, 4}, 512, 1, "site/tile1x4x8x16/512thr/1blk/f32x2", 1},
 		    {2, {1, 2, 2, 4}, 512, 1, "site/tile2x4x4x16/512thr/1blk/f32x2", 1},
-		    {2, {1, 1, 3, 3}, 256, 2, "site/tile2x2x8x8/256thr/2blk/f32x2", 1}};
+		    {2, {1, 1, 3, 3}, 256, 2, "site/tile2x2x8x8/256thr/2blk/f32x2", 1},
+		    {2, {0, 1, 4, 4}, 512, 1, "site/tile1x2x16x16/512thr/1blk/f32x2", 1},
+		    {2, {1, 1, 2, 5}, 512, 1, "site/tile2x2x4x32/512thr/1blk/f32x2", 1},
+		    {2, {0, 2, 2, 5}, 512, 1, "site/tile1x4x4x32/512thr/1blk/f32x2", 1},
+		    {2, {0, 1, 3, 5}, 512, 1, "site/tile1x2x8x32/512thr/1blk/f32x2", 1}};
 		return t[v];
 	}
 	static bool force_variant_valid(Geom const &g, int v)
@@ -2257,7 +2261,7 @@ template <int GRP, class T, int ND> struct Ops
 		return ts;
 	}
 	// ---- fused momentum step + link update (trajectory) ----------------------
-	static constexpr int kMdFirst = 14, kMdLast = 53; // thread-per-site and line-march variants
+	static constexpr int kMdFirst = 14, kMdLast = 57; // thread-per-site and line-march variants
 	static bool md_supported(Geom const &g)
 	{
 		if constexpr (ND != 4)

@@ -194,7 +194,7 @@ def test_exp_fp32_series_and_closed_form(ctx, oracle, g, t):
     assert rel(U.export(), oracle.evolve(g, 2, dims, U64, P64, t)) < TOL32
 
 
-@pytest.mark.parametrize("variant", list(range(54)))
+@pytest.mark.parametrize("variant", list(range(58)))
 @pytest.mark.parametrize("g,p", [(3, 1), (3, 2), (2, 1), (1, 1)])
 def test_every_force_launch_variant_vs_oracle(ctx, oracle, g, p, variant):
     """each launch variant the autotuner can choose (thread per link in
@@ -345,7 +345,7 @@ def test_pinned_host_transfers_match_staged(ctx, oracle, monkeypatch, g, p, dims
         assert np.array_equal(out2.numpy(), staged)
 
 
-@pytest.mark.parametrize("variant", [-1, 11, 13, 14, 15, 16, 17, 18, 20, 21, 22, 23, 25, 29, 30, 31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53])
+@pytest.mark.parametrize("variant", [-1, 11, 13, 14, 15, 16, 17, 18, 20, 21, 22, 23, 25, 29, 30, 31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53, 54, 55, 56, 57])
 @pytest.mark.parametrize("g", [2, 3])
 def test_trajectory_momentum_step_matches_generic(ctx, oracle, g, variant):
     """the trajectory's momentum step (SU(3) FP32 links read as rows 0, 1 with
@@ -393,7 +393,7 @@ def test_md_step_vs_oracle(ctx, oracle, g, p):
     assert rel(h.U.export(), U_o) < 2 * tol(p)
 
 
-MD_VARIANTS = [(3, v) for v in (-1, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53)] + [(g, v) for g in (1, 2) for v in (-1, 18, 20)]
+MD_VARIANTS = [(3, v) for v in (-1, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 33, 34, 35, 36, 37, 38, 39, 40, 41, 42, 43, 44, 45, 46, 47, 48, 49, 50, 51, 52, 53, 54, 55, 56, 57)] + [(g, v) for g in (1, 2) for v in (-1, 18, 20)]
 
 
 @pytest.mark.parametrize("g,variant", MD_VARIANTS)
