@@ -10,13 +10,15 @@ replaced by 10 overrelaxation sweeps.
 Cost = descent steps + 11 per fallback (a fallback is 10 sweeps plus the
 rejected step); overrelaxation costs one per sweep. A sweep and a descent
 step take about the same time, so the comparisons do not depend on timing
-noise. Measured on a GB300 on these eight configurations: overrelaxation
-55200, plain multiplier 16317, the best fixed member of the training family
-(alpha 0.08, high-mode factor 0.6) 20431, the network 18910.
+noise. Measured on a GB300 on these eight configurations when the network
+was committed: overrelaxation 55200, plain multiplier 16317, the best fixed
+member of the training family (alpha 0.08, high-mode factor 0.6) 20431, the
+network 18910 (the configurations depend on the HMC kernels' rounding, so a
+later build generates slightly different ones).
 
 * Fourier-accelerated descent with the network reaches theta < 1e-12 on
   every configuration, at a third of the cost of FP64 overrelaxation (the
-  the benchmark spec target: at least 2x less).
+  target is at least 2x less).
 * The network does beat the fixed family member it was trained against on
   the sum (0.93x its cost) but not the plain multiplier (1.16x): the cost of
   one configuration varies up to 4x with either multiplier, the per-decade
