@@ -3,8 +3,9 @@
 special unitary matrices and algebra elements: the row-2 rebuild
 conj(row 0 x row 1) with fused multiply-adds, the projection from rows 0, 1
 (proj_rows01), the order-6/order-10 exponential series and the rows-0,1
-exponential of the fused link update. FP32 results within 4e-7 of FP64; the
-row-2-free projection within 1e-14 in FP64. No GPU needed."""
+exponential of the fused link update, and the four-dimensional plane tables.
+FP32 results within 4e-7 of FP64; the row-2-free projection within 1e-14 in
+FP64. No GPU needed."""
 import os
 import shutil
 import subprocess
@@ -59,7 +60,12 @@ int main()
 		for (int k = 0; k < 12; ++k)
 			e_exp_rows = std::fmax(e_exp_rows, std::fabs(double(z.v[k]) - x.v[k]));
 	}
-	std::printf("%.3e %.3e %.3e %.3e\n", e_row2, e_proj01, e_exp, e_exp_rows);
+	// the four-dimensional plane tables against the enumeration (0,1), (0,2), ...
+	int q = 0, bad_planes = 0;
+	for (int mu = 0; mu < 4; ++mu)
+		for (int nu = mu + 1; nu < 4; ++nu, ++q)
+			bad_planes += plane_mu<4>(q) != mu || plane_nu<4>(q) != nu;
+	std::printf("%.3e %.3e %.3e %.3e %d\n", e_row2, e_proj01, e_exp, e_exp_rows, bad_planes);
 	return 0;
 }
 """
@@ -79,7 +85,8 @@ def test_su3_fp32_helpers_against_fp64(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
-    e_row2, e_proj01, e_exp, e_exp_rows = (float(v) for v in out.stdout.split())
+    e_row2, e_proj01, e_exp, e_exp_rows, bad_planes = (float(v) for v in out.stdout.split())
+    assert bad_planes == 0
     assert e_row2 < 4e-7
     assert e_proj01 < 1e-14
     assert e_exp < 4e-7
